@@ -1,0 +1,457 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 stable LSD radix sort (one JSON line on stdout, rank 0).
+
+Workload (one step): the mode/dtype sweep at 2^28 keys, one array each --
+  * float32 N(0, 1e3) with 1% -0.0, 0.5% +-inf, 0.1% NaN, sorted descending with the
+    absolute filter (rsbd8::radixsortcopy<dscfwdorder, nativeabs>);
+  * int64 uniform over the full signed range, ascending;
+  * uint32 with only the low 12 bits random (the pass-skip test drops two digits), ascending.
+Synthetic seeded data of exactly those shapes (no dataset exists for this benchmark).
+
+value      device-resident throughput: keys sorted per second over the K timed steps
+           (inputs already in HBM, radixsortcopynoalloc with preallocated buffers; every input
+           is larger than the 129 MB L2, so no flush is needed between steps);
+e2e        the same sorts through the C ABI from pinned HOST buffers: each step copies the
+           inputs host->device, sorts, and copies the sorted arrays back;
+roofline   the dominant kernel (the onesweep scatter pass on 64-bit keys): algorithmic bytes per
+           launch (2 x 8 B x 2^28: read + write of one pass) / its average launch time, measured
+           with CUDA events on the launch stream inside the timed region, against the measured
+           HBM copy bandwidth;
+cpu_baseline  the oracle's multithreaded C port of the reference's LSD sort on a bounded sample,
+           on the host cores of the same machine.
+`--impl reference` times that CPU implementation as the reference arm.
+With --gpus N (launched under torchrun) every rank sorts its own copy of the workload
+(replicas: the sort has no exchange step) and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+SEEDS = {"f32": 0x5EED0002, "i64": 0x5EED0003, "u32low12": 0x5EED0004, "u32": 0x5EED0005}
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--log2n", type=int, default=28, help="keys per array (2^log2n)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(log2n: int) -> dict:
+    return {"workload": f"mode/dtype sweep, 3 arrays x 2^{log2n} keys: float32 N(0,1e3)+specials "
+                        f"dscfwdorder nativeabs; int64 uniform ascfwdorder; uint32 low-12-bit ascfwdorder",
+            "keys_per_step": 3 * (1 << log2n), "api": "radixsortcopynoalloc (C ABI)",
+            "l2": "inputs larger than L2 (>= 1 GiB per array), no flush",
+            "parallelism": "replicas (no exchange step)"}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "onesweep_u64_int64_2p28_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_full_size:"):
+                    return float(line.split(":", 1)[1])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={CLOCK_FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---- the workload ------------------------------------------------------------------------
+
+def make_arrays(log2n: int, device):
+    """Device-resident inputs of the sweep: (name, bits tensor, key dtype, direction, mode)."""
+    import numpy as np
+    from radixsortbidi8_gb300 import synth as S
+    n = 1 << log2n
+    return [
+        ("float32_abs_dscfwdorder", S.float_specials_torch(SEEDS["f32"], n, 4, device=device), np.float32,
+         "dscfwdorder", "nativeabs"),
+        ("int64_ascfwdorder", S.uniform_bits_torch(SEEDS["i64"], n, 8, device=device), np.int64,
+         "ascfwdorder", "native"),
+        ("uint32_low12_ascfwdorder", S.low_bits_u32_torch(SEEDS["u32low12"], n, device=device), np.uint32,
+         "ascfwdorder", "native"),
+    ]
+
+
+def active_passes(bits, name: str) -> int:
+    """Digits the pass-skip test keeps: bytes of the filtered key that are not constant."""
+    import torch
+    x = bits
+    if name.startswith("float32_abs"):
+        x = x & 0x7FFFFFFF                      # the absolute filter drops the sign bit
+    kb = x.element_size()
+    cnt = 0
+    for p in range(kb):
+        d = (x >> (8 * p)) & 0xFF
+        if int(d.min()) != int(d.max()):
+            cnt += 1
+    del torch
+    return cnt
+
+
+def gb300_arm(args, rank: int, world: int):
+    import numpy as np
+    import torch
+    import radixsortbidi8_gb300 as rs
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    rs.lib()
+    n = 1 << args.log2n
+    arrays = make_arrays(args.log2n, dev)
+    stream = torch.cuda.Stream(device=dev)
+    bufs = []
+    for name, bits, kdt, d, m in arrays:
+        nb = rs.scratch_bytes(kdt, n, d, m)
+        bufs.append((torch.empty_like(bits), torch.empty_like(bits),
+                     torch.empty(nb, dtype=torch.uint8, device=dev)))
+    act = [active_passes(b, nm) for nm, b, *_ in arrays]
+    torch.cuda.synchronize()
+
+    def step():
+        for (name, bits, kdt, d, m), (out, buf, scr) in zip(arrays, bufs):
+            rs.radixsortcopynoalloc(bits, out, buf, scr, d, m, key_dtype=kdt, stream=stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    for (out, buf, scr) in bufs:
+        assert rs.scratch_status(scr, stream) == 0
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    rs.api.profile_enable(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    rs.api.profile_enable(False)
+    barrier()
+    clk = clocks.stop()
+    ms_total = t0.elapsed_time(t1)
+    recs = rs.api.profile_collect()
+    for (out, buf, scr) in bufs:
+        assert rs.scratch_status(scr, stream) == 0
+
+    # correctness of the timed outputs: sorted by the filtered key, same multiset of bits
+    check = verify_outputs(arrays, bufs)
+
+    ms_step = ms_total / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    keys_step = 3 * n
+    value = world * keys_step / (ms_step * 1e-3) / 1e9
+
+    peak, peak_kind = measured_peak()
+    # per-sort and per-kernel breakdown from the launch records (launch order is fixed per step)
+    per_sort = {nm: {"ms": 0.0, "sweep_ms": [], "launches": 0} for nm, *_ in arrays}
+    ours = [r for r in recs if r["kernel"] != "memset"]
+    order = []
+    for nm, bits, *_ in arrays:
+        order += [nm] * (3 + 1 + bits.element_size())  # memset, histogram, plan, passes, copy
+    for i, r in enumerate(recs):
+        nm = order[i % len(order)]
+        per_sort[nm]["ms"] += r["ms"]
+        if r["kernel"] != "memset":
+            per_sort[nm]["launches"] += 1
+        if r["kernel"] == "onesweep":
+            per_sort[nm]["sweep_ms"].append((r["pass_"], r["ms"]))
+    per_dtype = {}
+    for (nm, bits, kdt, d, m), a in zip(arrays, act):
+        kb = bits.element_size()
+        t = per_sort[nm]["ms"] / args.steps
+        algo = a * 2 * kb * n
+        per_dtype[nm] = {"gkeys_s": round(n / (t * 1e-3) / 1e9, 3), "ms": round(t, 4), "active_passes": a,
+                         "algorithmic_bytes": algo,
+                         "roofline_frac": round(algo / (t * 1e-3) / 1e9 / peak, 4)}
+    # dominant kernel: onesweep on the 64-bit keys (every pass active)
+    sw = [ms for p, ms in per_sort["int64_ascfwdorder"]["sweep_ms"]]
+    avg_ms = sum(sw) / len(sw)
+    bytes_launch = 2 * 8 * n
+    achieved = bytes_launch / (avg_ms * 1e-3) / 1e9
+    share = {k: 0.0 for k in ("memset", "histogram", "plan", "onesweep", "copy")}
+    for r in recs:
+        share[r["kernel"]] = share.get(r["kernel"], 0.0) + r["ms"]
+    tot = sum(share.values())
+    roofline = {"bound": "hbm", "kernel": "k_onesweep<uint64> (int64 sort, 8 active passes)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"of {peak_kind}",
+                "traffic": profiled_traffic(), "bytes_per_launch": bytes_launch,
+                "avg_launch_ms": round(avg_ms, 4),
+                "time_share": {k: round(v / tot, 4) for k, v in share.items() if tot}}
+
+    extra = uniform_u32(args, rs, dev, stream, peak)
+    e2e = None if args.no_e2e else e2e_arm(args, rs, arrays, stream)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(arrays, min(args.log2n, 24))
+    line = {
+        "metric": "GKeys/s", "value": round(value, 3), "unit": "GKeys/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/i64/u32 keys (integer ops)",
+        "data": "synthetic (seeded splitmix64; shapes and distributions of the benchmark configuration)",
+        "config": workload_config(args.log2n),
+        "roofline": roofline, "per_dtype": per_dtype, "uint32_uniform_2p28": extra,
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": len(ours), "checked": check,
+    }
+    return line
+
+
+def verify_outputs(arrays, bufs) -> str:
+    """Sortedness by the filtered key and equal bit multisets (sum and xor of the bits)."""
+    import torch
+    for (nm, bits, kdt, d, m), (out, buf, scr) in zip(arrays, bufs):
+        x = out
+        if nm.startswith("float32_abs"):
+            k = (x & 0x7FFFFFFF).to(torch.int64)
+            ok = bool((k[:-1] >= k[1:]).all())                      # descending |x|
+        elif nm.startswith("int64"):
+            ok = bool((x[:-1] <= x[1:]).all())
+        else:
+            k = x.to(torch.int64) & 0xFFFFFFFF
+            ok = bool((k[:-1] <= k[1:]).all())
+        s1 = int(bits.to(torch.int64).sum()) == int(x.to(torch.int64).sum())
+        if not (ok and s1):
+            return f"FAILED {nm}"
+    return "sorted by filtered key; bit sums equal"
+
+
+def uniform_u32(args, rs, dev, stream, peak) -> dict:
+    """2^28 uniform uint32 keys (4 active passes): the 70%-of-roofline target, measured alone."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import synth as S
+    n = 1 << args.log2n
+    bits = S.uniform_bits_torch(SEEDS["u32"], n, 4, device=dev)
+    out, buf = torch.empty_like(bits), torch.empty_like(bits)
+    scr = torch.empty(rs.scratch_bytes(np.uint32, n), dtype=torch.uint8, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            rs.radixsortcopynoalloc(bits, out, buf, scr, key_dtype=np.uint32, stream=stream)
+    torch.cuda.synchronize()
+    rs.api.profile_enable(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        rs.radixsortcopynoalloc(bits, out, buf, scr, key_dtype=np.uint32, stream=stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    rs.api.profile_enable(False)
+    recs = rs.api.profile_collect()
+    ms = t0.elapsed_time(t1) / args.steps
+    sw = [r["ms"] for r in recs if r["kernel"] == "onesweep"]
+    hist = [r["ms"] for r in recs if r["kernel"] == "histogram"]
+    algo = 4 * 2 * 4 * n
+    k = out.to(torch.int64) & 0xFFFFFFFF
+    ok = bool((k[:-1] <= k[1:]).all())
+    del bits, out, buf, scr
+    return {"gkeys_s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4),
+            "roofline_frac": round(algo / (ms * 1e-3) / 1e9 / peak, 4),
+            "onesweep_avg_ms": round(sum(sw) / len(sw), 4),
+            "onesweep_GBps": round(2 * 4 * n / (sum(sw) / len(sw) * 1e-3) / 1e9, 1),
+            "histogram_ms": round(sum(hist) / len(hist), 4), "sorted": ok}
+
+
+def e2e_arm(args, rs, arrays, stream) -> dict:
+    """Host buffers in, host buffers out, through the C ABI: H2D + sort + D2H every step."""
+    import torch
+    steps = max(1, min(args.steps, 5))
+    host_in = [b.cpu().pin_memory() for _, b, *_ in arrays]
+    host_out = [torch.empty_like(h).pin_memory() for h in host_in]
+    dev_in = [torch.empty_like(b) for _, b, *_ in arrays]
+    dev_out = [torch.empty_like(b) for _, b, *_ in arrays]
+    dev_buf = [torch.empty_like(b) for _, b, *_ in arrays]
+    n = arrays[0][1].numel()
+    scr = [torch.empty(rs.scratch_bytes(kdt, n, d, m), dtype=torch.uint8, device=b.device)
+           for _, b, kdt, d, m in arrays]
+    h2d = sum(h.numel() * h.element_size() for h in host_in)
+
+    def one():
+        for i, (nm, b, kdt, d, m) in enumerate(arrays):
+            dev_in[i].copy_(host_in[i], non_blocking=True)
+            rs.radixsortcopynoalloc(dev_in[i], dev_out[i], dev_buf[i], scr[i], d, m, key_dtype=kdt, stream=stream)
+            host_out[i].copy_(dev_out[i], non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        one()
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            one()
+        t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    return {"value": round(3 * n / (ms * 1e-3) / 1e9, 3), "unit": "GKeys/s", "ms_per_step": round(ms, 3),
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "steps": steps,
+            "path": "pinned host -> cudaMemcpyAsync -> radixsortcopynoalloc -> cudaMemcpyAsync -> pinned host"}
+
+
+def cpu_sample_arrays(log2n_sample: int):
+    """Host copies of the first 2^k keys of each array (numpy, same generators)."""
+    import numpy as np
+    from radixsortbidi8_gb300 import synth as S
+    n = 1 << log2n_sample
+    return [
+        (S.float_specials(SEEDS["f32"], n, np.float32), "nativeabs", "dscfwdorder"),
+        (S.uniform_bits(SEEDS["i64"], n, np.int64), "native", "ascfwdorder"),
+        (S.low_bits_u32(SEEDS["u32low12"], n), "native", "ascfwdorder"),
+    ]
+
+
+def cpu_baseline(arrays, log2n_sample: int, reps: int = 3) -> dict:
+    """The oracle's multithreaded C port of the reference LSD sort on a bounded sample."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    samples = cpu_sample_arrays(log2n_sample)
+    best = float("inf")
+    for _ in range(reps):
+        t = time.perf_counter()
+        for a, m, d in samples:
+            O.sortcopy(a, m, d, threads=threads)
+        best = min(best, time.perf_counter() - t)
+    keys = sum(a.size for a, *_ in samples)
+    return {"value": round(keys / best / 1e9, 4), "unit": "GKeys/s", "cores": threads, "kind": "port",
+            "sample": f"first 2^{log2n_sample} keys of each of the 3 arrays (same generators), best of {reps}"}
+
+
+def reference_arm(args, rank: int, world: int) -> dict | None:
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    k = min(args.log2n, 24)
+    samples = cpu_sample_arrays(k)
+    for _ in range(args.warmup):
+        for a, m, d in samples:
+            O.sortcopy(a, m, d, threads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        for a, m, d in samples:
+            O.sortcopy(a, m, d, threads=threads)
+    el = time.perf_counter() - t
+    keys = args.steps * sum(a.size for a, *_ in samples)
+    v = keys / el / 1e9
+    return {"metric": "GKeys/s", "value": round(v, 4), "unit": "GKeys/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/i64/u32 keys (integer ops)",
+            "data": "synthetic (seeded splitmix64)", "config": workload_config(args.log2n), "impl": "reference",
+            "cpu_baseline": {"value": round(v, 4), "unit": "GKeys/s", "cores": threads, "kind": "port",
+                             "sample": f"each step sorts the first 2^{k} keys of each of the 3 arrays"},
+            "e2e": {"value": round(v, 4), "unit": "GKeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's CPU algorithm as the oracle's multithreaded C port (the reference's own "
+                    "compiled code does not travel to this host)"}
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1 and args.impl == "gb300":
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        line = reference_arm(args, rank, world)
+    else:
+        line = gb300_arm(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and args.impl == "gb300":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

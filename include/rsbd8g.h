@@ -1,0 +1,171 @@
+/*
+ * rsbd8g.h - C ABI of the GB300 (sm_103a) stable LSD radix sort.
+ *
+ * A device-resident drop-in for the sorting entry points of the Radixsortbidi8
+ * library (header Radixsortbidi8.hpp, namespace rsbd8).  Every entry point takes
+ * plain device pointers and sizes; no C++ or CUDA type crosses this boundary.
+ * The C++ template facade in rsbd8.hpp maps the reference's template
+ * parameters (key type, sortingmode, sortingdirection, member pointer or
+ * type+offset indirection) onto rsbd8g_desc and calls these functions.
+ *
+ * Semantics are those of the reference: a stable sort by the filtered key of the
+ * selected sortingmode, ascending or descending, with ties in input order
+ * (forward) or reversed (reverse order), where the reference honours it.
+ *
+ * Stream use: every call is ordered on the given stream (NULL = the legacy
+ * default stream).  The allocating forms (rsbd8g_radixsort, rsbd8g_radixsortcopy)
+ * block until the sort is complete, as the reference's functions do, and report
+ * device-side errors.  The noalloc forms only enqueue work; call
+ * rsbd8g_scratch_status() to wait and read the device-side status word.
+ */
+#ifndef RSBD8G_H
+#define RSBD8G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define RSBD8G_API __attribute__((visibility("default")))
+#else
+#define RSBD8G_API
+#endif
+
+/* an opaque CUDA stream handle; pass a cudaStream_t (or CUstream) here */
+typedef struct CUstream_st *rsbd8g_stream;
+
+typedef enum rsbd8g_status {
+    RSBD8G_OK = 0,
+    RSBD8G_ERR_BAD_ARG = 1,      /* null pointer, aliasing, bad mode/direction/key size, scratch too small */
+    RSBD8G_ERR_NO_MEMORY = 2,    /* device allocation failed (the reference returns false here) */
+    RSBD8G_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    RSBD8G_ERR_TIMEOUT = 4,      /* a bounded device-side wait ran out (the look-back of the scatter) */
+    RSBD8G_ERR_DEVICE_FAULT = 5, /* the device flagged an internal inconsistency */
+    RSBD8G_ERR_TOO_LARGE = 6,    /* count beyond the supported range */
+    RSBD8G_ERR_BUSY = 7          /* serving: admission refused, the memory budget is exhausted */
+} rsbd8g_status;
+
+/* what std::is_signed_v / std::is_floating_point_v report for the key type:
+ * enumerations, bool and classes are RSBD8G_KIND_UNSIGNED, as in the reference */
+enum { RSBD8G_KIND_UNSIGNED = 0, RSBD8G_KIND_SIGNED = 1, RSBD8G_KIND_FLOAT = 2 };
+
+/* rsbd8::sortingmode values (Radixsortbidi8.hpp:212-250) */
+enum {
+    RSBD8G_MODE_FORCEUNSIGNED = 0, RSBD8G_MODE_SPECIALSIGNED = 0,
+    RSBD8G_MODE_FORCETIEREDABSSIGNED = 1, RSBD8G_MODE_FORCESIGNED = 2,
+    RSBD8G_MODE_FORCEABSSIGNED = 3, RSBD8G_MODE_SPECIALFLOATINGP = 4,
+    RSBD8G_MODE_FORCETIEREDABSFLOATINGP = 5, RSBD8G_MODE_FORCEFLOATINGP = 6,
+    RSBD8G_MODE_FORCEABSFLOATINGP = 7, RSBD8G_MODE_SPECIALUNSIGNED = 7,
+    RSBD8G_MODE_NATIVE = 64, RSBD8G_MODE_NATIVEABS = 65, RSBD8G_MODE_NATIVETIEREDABS = 66
+};
+
+/* rsbd8::sortingdirection values (Radixsortbidi8.hpp:252-265) */
+enum {
+    RSBD8G_ASCFWDORDER = 0, RSBD8G_DSCFWDORDER = 1,
+    RSBD8G_ASCREVORDER = 2, RSBD8G_DSCREVORDER = 3
+};
+
+/* indirection kinds */
+enum {
+    RSBD8G_DIRECT = 0,      /* the arrays hold the keys themselves */
+    RSBD8G_MEMBER = 1,      /* the arrays hold object pointers; the key is at byte offset1 of each object
+                               (member object pointer or type+offset form) */
+    RSBD8G_MEMBER2 = 2      /* second level: the object holds a pointer at byte offset1, and the key
+                               sits at byte offset2 behind that pointer */
+};
+
+/* diagnostics only: tile 1 of every scatter pass never publishes its look-back state, so
+ * the tiles after it run into the bounded device-side wait (200 ms) and the call reports
+ * RSBD8G_ERR_TIMEOUT with the output undefined; the device stays usable */
+#define RSBD8G_FLAG_DIAG_STALL 1u
+
+typedef struct rsbd8g_desc {
+    uint32_t key_bytes;     /* 1, 2, 4 or 8 */
+    uint32_t key_kind;      /* RSBD8G_KIND_* */
+    uint32_t mode;          /* rsbd8::sortingmode value */
+    uint32_t direction;     /* rsbd8::sortingdirection value */
+    uint32_t indirection;   /* RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2 */
+    uint32_t flags;         /* 0, or RSBD8G_FLAG_* diagnostics */
+    int64_t offset1;        /* RSBD8G_MEMBER*: byte offset of the key (or second pointer) in each object */
+    int64_t offset2;        /* RSBD8G_MEMBER2: byte offset of the key behind the second pointer */
+} rsbd8g_desc;
+
+/* Scratch bytes the noalloc forms need for `count` elements (the index counts,
+ * look-back state and, for indirection, the gathered keys).  The ping-pong
+ * buffer of `count` elements is separate, as in the reference.
+ * Replaces: rsbd8::allocatearray sizing (Radixsortbidi8.hpp:59928). */
+RSBD8G_API rsbd8g_status rsbd8g_scratch_bytes(const rsbd8g_desc *desc, size_t count, size_t *bytes);
+
+/* Sort `count` elements of `input` into `output` (input is not written).
+ * Allocates its scratch and buffer on the stream, blocks until done.
+ * Replaces: rsbd8::radixsortcopy (Radixsortbidi8.hpp:60476, single-part :60536;
+ * member pointer :61242; type+offset :61359-61739). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy(const rsbd8g_desc *desc, size_t count,
+                                              const void *input, void *output, rsbd8g_stream stream);
+
+/* Sort `count` elements of `input` in place.  Allocates, blocks until done.
+ * Replaces: rsbd8::radixsort (Radixsortbidi8.hpp:60398). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsort(const rsbd8g_desc *desc, size_t count, void *input,
+                                          rsbd8g_stream stream);
+
+/* Sort into `output` with caller-provided `buffer` (count elements) and `scratch`
+ * (rsbd8g_scratch_bytes, any content: the call clears what it needs).
+ * Stream-ordered: returns after enqueueing.
+ * Replaces: rsbd8::radixsortcopynoalloc (Radixsortbidi8.hpp:60129; indirect :60983);
+ * the reference's allowedthreads / pfuturesplaceholder have no GPU meaning and
+ * `scratch` takes the place of pzeroedindices. */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopynoalloc(const rsbd8g_desc *desc, size_t count,
+                                                     void *scratch, size_t scratch_bytes,
+                                                     const void *input, void *output, void *buffer,
+                                                     rsbd8g_stream stream);
+
+/* In-place sort of `input` using `buffer` (count elements); the result lands in
+ * `input`, or in `buffer` when movetobuffer is non-zero (the other array then
+ * holds garbage).  Stream-ordered.
+ * Replaces: rsbd8::radixsortnoalloc (Radixsortbidi8.hpp:60163; indirect :61018). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t count,
+                                                 void *scratch, size_t scratch_bytes,
+                                                 void *input, void *buffer, int movetobuffer,
+                                                 rsbd8g_stream stream);
+
+/* Wait for the stream, then read and clear the device-side status word of a
+ * scratch area used by a noalloc call (RSBD8G_OK, RSBD8G_ERR_TIMEOUT, ...). */
+RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stream);
+
+/* Human-readable name of a status code. */
+RSBD8G_API const char *rsbd8g_status_string(rsbd8g_status status);
+
+/* ---- launch profiling (measurement support; no counterpart in the reference) ---------- */
+
+enum {
+    RSBD8G_KERNEL_MEMSET = 0, RSBD8G_KERNEL_HISTOGRAM = 1, RSBD8G_KERNEL_PLAN = 2,
+    RSBD8G_KERNEL_ONESWEEP = 3, RSBD8G_KERNEL_COPY = 4, RSBD8G_KERNEL_SEGMENTED = 5
+};
+
+typedef struct rsbd8g_launch_record {
+    uint32_t kernel;      /* RSBD8G_KERNEL_* */
+    uint32_t key_bytes;
+    uint32_t pass;        /* digit index of an onesweep launch */
+    uint32_t reserved;
+    uint64_t count;       /* elements of the sort the launch belongs to */
+    double ms;            /* device time between CUDA events recorded around the launch on its stream */
+} rsbd8g_launch_record;
+
+/* While enabled, every kernel launch of the library (outside stream capture) is bracketed
+ * by CUDA events on the stream it is launched on. */
+RSBD8G_API rsbd8g_status rsbd8g_profile_enable(int enable);
+
+/* Wait for the recorded events, copy up to `capacity` records (oldest first), report the
+ * number recorded in *count, and forget them. */
+RSBD8G_API rsbd8g_status rsbd8g_profile_collect(rsbd8g_launch_record *records, size_t capacity, size_t *count);
+
+/* Library version: major * 10000 + minor * 100 + patch. */
+RSBD8G_API int rsbd8g_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSBD8G_H */

@@ -1,0 +1,449 @@
+// rsbd8g_api.cu - host side of the C ABI declared in include/rsbd8g.h.
+//
+// Mode resolution restates helper::isabsvalue / issignmode / isfltpmode / isdescsort /
+// isrevorderwithindirection / isrevorderwithoutindirection (Radixsortbidi8.hpp:59778-59904);
+// the call sequence per sort is
+//   memset(control, histograms, look-back state) -> histogram (or gather+histogram)
+//   -> plan (scan + pass-skip + ping-pong) -> one onesweep pass per digit -> copy step,
+// all on the caller's stream, with no host synchronisation in between (a skipped pass
+// returns at once on the device), so the sequence can be captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "rsbd8g.h"
+#include "rsbd8g_internal.h"
+#include "rsbd8g_kernels.cuh"
+
+namespace rsbd8g {
+
+namespace {
+
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+constexpr uint64_t kMaxCount = uint64_t(1) << 40;
+constexpr uint64_t kNarrowStatusLimit = uint64_t(1) << 30;  // 30-bit look-back counts below this
+
+// tile geometry of the onesweep pass (keys per tile = THREADS * ITEMS)
+constexpr int kSweepThreads = 512;
+constexpr int kSweepItemsDirect = 16;
+constexpr int kSweepItemsIndirect = 8;
+constexpr int kHistThreads = 512;
+
+int device_sms(int dev) {
+    static int cache[64] = {0};
+    if (dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = v > 0 ? v : 152;
+    }
+    return cache[dev];
+}
+
+}  // namespace
+
+// ---- launch profiling -----------------------------------------------------------------------
+
+namespace {
+struct ProfRec {
+    rsbd8g_launch_record r;
+    cudaEvent_t a, b;
+};
+struct ProfState {
+    std::mutex mu;
+    bool on = false;
+    std::vector<ProfRec> recs;
+    std::vector<cudaEvent_t> pool;
+};
+ProfState &prof() {
+    static ProfState p;
+    return p;
+}
+cudaEvent_t prof_event() {
+    ProfState &p = prof();
+    if (!p.pool.empty()) {
+        cudaEvent_t e = p.pool.back();
+        p.pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+// run `launch` (which enqueues one kernel on s), bracketed by events while profiling is on
+template <class F>
+cudaError_t timed_launch(cudaStream_t s, uint32_t kernel, uint32_t key_bytes, uint32_t pass, uint64_t n, F &&launch) {
+    ProfState &p = prof();
+    bool on;
+    {
+        std::lock_guard<std::mutex> g(p.mu);
+        on = p.on;
+    }
+    if (on) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        if (cs != cudaStreamCaptureStatusNone) on = false;
+    }
+    if (!on) {
+        launch();
+        return cudaGetLastError();
+    }
+    cudaEvent_t a, b;
+    {
+        std::lock_guard<std::mutex> g(p.mu);
+        a = prof_event();
+        b = prof_event();
+    }
+    cudaEventRecord(a, s);
+    launch();
+    cudaError_t e = cudaGetLastError();
+    cudaEventRecord(b, s);
+    std::lock_guard<std::mutex> g(p.mu);
+    ProfRec pr{};
+    pr.r.kernel = kernel;
+    pr.r.key_bytes = key_bytes;
+    pr.r.pass = pass;
+    pr.r.count = n;
+    pr.a = a;
+    pr.b = b;
+    p.recs.push_back(pr);
+    return e;
+}
+
+rsbd8g_status profile_enable(int enable) {
+    std::lock_guard<std::mutex> g(prof().mu);
+    prof().on = enable != 0;
+    return RSBD8G_OK;
+}
+
+rsbd8g_status profile_collect(rsbd8g_launch_record *out, size_t cap, size_t *count) {
+    ProfState &p = prof();
+    std::lock_guard<std::mutex> g(p.mu);
+    if (count) *count = p.recs.size();
+    rsbd8g_status st = RSBD8G_OK;
+    for (size_t i = 0; i < p.recs.size(); ++i) {
+        ProfRec &pr = p.recs[i];
+        float ms = 0.f;
+        if (cudaEventSynchronize(pr.b) != cudaSuccess || cudaEventElapsedTime(&ms, pr.a, pr.b) != cudaSuccess)
+            st = RSBD8G_ERR_CUDA;
+        pr.r.ms = ms;
+        if (out && i < cap) out[i] = pr.r;
+        p.pool.push_back(pr.a);
+        p.pool.push_back(pr.b);
+    }
+    p.recs.clear();
+    return st;
+}
+
+rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
+    if (!d || !r) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_bytes != 1 && d->key_bytes != 2 && d->key_bytes != 4 && d->key_bytes != 8) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_kind > RSBD8G_KIND_FLOAT) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_kind == RSBD8G_KIND_FLOAT && d->key_bytes < 4) return RSBD8G_ERR_BAD_ARG;
+    const uint32_t mode = d->mode, dir = d->direction;
+    if (!(mode < 8u || (mode >= 64u && mode <= 66u))) return RSBD8G_ERR_BAD_ARG;
+    if (dir > 3u) return RSBD8G_ERR_BAD_ARG;
+    if (d->indirection > RSBD8G_MEMBER2) return RSBD8G_ERR_BAD_ARG;
+    const bool is_signed = d->key_kind == RSBD8G_KIND_SIGNED || d->key_kind == RSBD8G_KIND_FLOAT;
+    const bool is_float = d->key_kind == RSBD8G_KIND_FLOAT;
+    Filter f;
+    f.absv = (mode >= 65u && is_signed) || (mode < 64u && (mode & 1u));
+    f.sign = (mode >= 64u && mode <= 65u && is_signed) || (mode < 64u && (mode & 2u));
+    f.fltp = (mode >= 64u && is_float) || (mode < 64u && (mode & 4u));
+    f.desc = dir & 1u;
+    r->f = f;
+    r->indirect = d->indirection;
+    r->rev = d->indirection ? ((dir >> 1) & 1u)
+                            : (((dir >> 1) & 1u) && ((f.absv && f.sign) || (!f.absv && f.sign && f.fltp)));
+    r->key_bytes = d->key_bytes;
+    r->elem_bytes = d->indirection ? 8u : d->key_bytes;
+    r->off1 = d->offset1;
+    r->off2 = d->offset2;
+    r->flags = d->flags;
+    return RSBD8G_OK;
+}
+
+Layout layout_for(const Resolved &r, uint64_t n) {
+    Layout L{};
+    const int tile = kSweepThreads * (r.indirect ? kSweepItemsIndirect : kSweepItemsDirect);
+    L.num_tiles = uint32_t((n + tile - 1) / tile);
+    L.wide_status = n >= kNarrowStatusLimit;
+    const size_t sw = L.wide_status ? 8 : 4;
+    const uint32_t passes = r.key_bytes;
+    L.ctrl = 0;
+    L.ghist = align_up(sizeof(Control));
+    L.bstart = L.ghist + align_up(size_t(kMaxPasses) * kBuckets * 8);
+    L.status = L.bstart + align_up(size_t(kMaxPasses) * kBuckets * 8);
+    L.status_pass_bytes = align_up(size_t(L.num_tiles) * kBuckets * sw);
+    L.zero_bytes = L.status + size_t(passes) * L.status_pass_bytes;
+    L.keys_a = L.zero_bytes;
+    const size_t kb = r.indirect ? align_up(size_t(n) * r.key_bytes) : 0;
+    L.keys_b = L.keys_a + kb;
+    L.total = L.keys_b + kb;
+    return L;
+}
+
+namespace {
+
+template <typename U, bool HAS_VAL, typename S>
+cudaError_t launch_sweeps(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, cudaStream_t s) {
+    constexpr int ITEMS = HAS_VAL ? kSweepItemsIndirect : kSweepItemsDirect;
+    using SM = OnesweepSmem<U, HAS_VAL, kSweepThreads, ITEMS>;
+    auto kern = k_onesweep<U, HAS_VAL, kSweepThreads, ITEMS, S>;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static std::once_flag once[64];
+    static int occ[64];
+    std::call_once(once[dev & 63], [&] {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SM::kBytes));
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSweepThreads, SM::kBytes);
+        occ[dev & 63] = b > 0 ? b : 1;
+    });
+    const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, uint64_t(occ[dev & 63]) * device_sms(dev)));
+    Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
+    const unsigned long long *bstart = reinterpret_cast<const unsigned long long *>(scratch + L.bstart);
+    const Filter f = r.f;
+    for (uint32_t p = 0; p < r.key_bytes; ++p) {
+        S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
+        cudaError_t e = timed_launch(s, RSBD8G_KERNEL_ONESWEEP, r.key_bytes, p, n, [&] {
+            kern<<<grid, kSweepThreads, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, f);
+        });
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <typename U>
+cudaError_t launch_histogram(const Resolved &r, uint64_t n, const void *in, const Layout &L, unsigned char *scratch,
+                             cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t per_cta = uint64_t(kHistThreads) * 64;   // keys per CTA sweep, to size the grid
+    const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per_cta - 1) / per_cta,
+                                                                            uint64_t(device_sms(dev)) * 4)));
+    unsigned long long *ghist = reinterpret_cast<unsigned long long *>(scratch + L.ghist);
+    return timed_launch(s, RSBD8G_KERNEL_HISTOGRAM, r.key_bytes, 0, n, [&] {
+        if (r.indirect) {
+            k_gather_histogram<U, kHistThreads><<<grid, kHistThreads, 0, s>>>(
+                static_cast<const uint64_t *>(in), n, r.f, r.off1, r.off2, int(r.indirect),
+                reinterpret_cast<U *>(scratch + L.keys_a), ghist);
+        } else {
+            k_histogram<U, kHistThreads><<<grid, kHistThreads, 0, s>>>(static_cast<const U *>(in), n, r.f, ghist);
+        }
+    });
+}
+
+template <typename U>
+cudaError_t launch_all(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in,
+                       void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
+    cudaError_t e = timed_launch(s, RSBD8G_KERNEL_MEMSET, r.key_bytes, 0, n,
+                                 [&] { cudaMemsetAsync(scratch, 0, L.zero_bytes, s); });
+    if (e != cudaSuccess) return e;
+    if ((e = launch_histogram<U>(r, n, in, L, scratch, s)) != cudaSuccess) return e;
+    PlanArgs a{};
+    a.in = in;
+    a.out = out;
+    a.buf = buf;
+    a.keys_a = r.indirect ? scratch + L.keys_a : nullptr;
+    a.keys_b = r.indirect ? scratch + L.keys_b : nullptr;
+    a.elem_bytes = r.elem_bytes;
+    a.inplace = inplace;
+    a.to_buffer = to_buffer;
+    a.rev = r.rev;
+    a.indirect = r.indirect != 0;
+    a.passes = r.key_bytes;
+    const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
+    a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
+    a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;
+    e = timed_launch(s, RSBD8G_KERNEL_PLAN, r.key_bytes, 0, n, [&] {
+        k_plan<<<1, 256, 0, s>>>(reinterpret_cast<Control *>(scratch + L.ctrl),
+                                 reinterpret_cast<const unsigned long long *>(scratch + L.ghist),
+                                 reinterpret_cast<unsigned long long *>(scratch + L.bstart), n, a);
+    });
+    if (e != cudaSuccess) return e;
+    if (r.indirect) {
+        e = L.wide_status ? launch_sweeps<U, true, uint64_t>(r, n, L, scratch, s)
+                          : launch_sweeps<U, true, uint32_t>(r, n, L, scratch, s);
+    } else {
+        e = L.wide_status ? launch_sweeps<U, false, uint64_t>(r, n, L, scratch, s)
+                          : launch_sweeps<U, false, uint32_t>(r, n, L, scratch, s);
+    }
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint32_t cgrid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(device_sms(dev)) * 8)));
+    return timed_launch(s, RSBD8G_KERNEL_COPY, r.key_bytes, 0, n, [&] {
+        k_copy<<<cgrid, 256, 0, s>>>(reinterpret_cast<const Control *>(scratch + L.ctrl), n);
+    });
+}
+
+}  // namespace
+
+rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
+                           void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
+    if (n > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
+    const Layout L = layout_for(r, n);
+    if (!scratch || scratch_bytes < L.total) return RSBD8G_ERR_BAD_ARG;
+    if ((reinterpret_cast<uintptr_t>(scratch) & (kAlign - 1)) != 0) return RSBD8G_ERR_BAD_ARG;
+    unsigned char *sc = static_cast<unsigned char *>(scratch);
+    cudaError_t e;
+    switch (r.key_bytes) {
+        case 1: e = launch_all<uint8_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 2: e = launch_all<uint16_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 4: e = launch_all<uint32_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        default: e = launch_all<uint64_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+    }
+    return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+}
+
+rsbd8g_status read_device_status(void *scratch, cudaStream_t s, bool clear) {
+    if (!scratch) return RSBD8G_ERR_BAD_ARG;
+    uint32_t err = 0;
+    Control *ctrl = static_cast<Control *>(scratch);
+    if (cudaMemcpyAsync(&err, &ctrl->error, sizeof err, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return RSBD8G_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return RSBD8G_ERR_CUDA;
+    if (clear && err) {
+        if (cudaMemsetAsync(&ctrl->error, 0, sizeof err, s) != cudaSuccess) return RSBD8G_ERR_CUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return RSBD8G_ERR_CUDA;
+    }
+    if (err & kDevTimeout) return RSBD8G_ERR_TIMEOUT;
+    if (err & kDevFault) return RSBD8G_ERR_DEVICE_FAULT;
+    return RSBD8G_OK;
+}
+
+}  // namespace rsbd8g
+
+// ---- the C ABI --------------------------------------------------------------------------------
+
+using namespace rsbd8g;
+
+extern "C" {
+
+RSBD8G_API int rsbd8g_version(void) { return 100; }
+
+RSBD8G_API rsbd8g_status rsbd8g_profile_enable(int enable) { return profile_enable(enable); }
+
+RSBD8G_API rsbd8g_status rsbd8g_profile_collect(rsbd8g_launch_record *records, size_t capacity, size_t *count) {
+    return profile_collect(records, capacity, count);
+}
+
+RSBD8G_API const char *rsbd8g_status_string(rsbd8g_status st) {
+    switch (st) {
+        case RSBD8G_OK: return "ok";
+        case RSBD8G_ERR_BAD_ARG: return "bad argument";
+        case RSBD8G_ERR_NO_MEMORY: return "device allocation failed";
+        case RSBD8G_ERR_CUDA: return "CUDA runtime error";
+        case RSBD8G_ERR_TIMEOUT: return "device-side wait timed out";
+        case RSBD8G_ERR_DEVICE_FAULT: return "device-side fault flag";
+        case RSBD8G_ERR_TOO_LARGE: return "count too large";
+        case RSBD8G_ERR_BUSY: return "admission refused: memory budget exhausted";
+    }
+    return "unknown status";
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_scratch_bytes(const rsbd8g_desc *desc, size_t count, size_t *bytes) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (!bytes) return RSBD8G_ERR_BAD_ARG;
+    if (count > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
+    *bytes = layout_for(r, count).total;
+    return RSBD8G_OK;
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopynoalloc(const rsbd8g_desc *desc, size_t count, void *scratch,
+                                                     size_t scratch_bytes, const void *input, void *output,
+                                                     void *buffer, rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (count == 0) return RSBD8G_OK;
+    if (!input || !output) return RSBD8G_ERR_BAD_ARG;
+    if (input == output) return RSBD8G_ERR_BAD_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (count == 1) {
+        return cudaMemcpyAsync(output, input, r.elem_bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+    }
+    if (!buffer || buffer == input || buffer == output) return RSBD8G_ERR_BAD_ARG;
+    return enqueue_sort(r, count, scratch, scratch_bytes, input, output, buffer, false, false, s);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t count, void *scratch,
+                                                 size_t scratch_bytes, void *input, void *buffer, int movetobuffer,
+                                                 rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (count == 0) return RSBD8G_OK;
+    if (!input) return RSBD8G_ERR_BAD_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (count == 1) {
+        if (!movetobuffer) return RSBD8G_OK;
+        if (!buffer) return RSBD8G_ERR_BAD_ARG;
+        return cudaMemcpyAsync(buffer, input, r.elem_bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+    }
+    if (!buffer || buffer == input) return RSBD8G_ERR_BAD_ARG;
+    return enqueue_sort(r, count, scratch, scratch_bytes, input, nullptr, buffer, true, movetobuffer != 0, s);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stream) {
+    return read_device_status(scratch, reinterpret_cast<cudaStream_t>(stream), true);
+}
+
+// allocating forms: one stream-ordered allocation of buffer + scratch, freed on the stream;
+// the call waits for the sort, as the reference's functions return only when sorted
+static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const void *input, void *output, bool inplace,
+                                rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (count > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (count <= 1) {
+        if (!inplace && count == 1) {
+            if (!input || !output || input == output) return RSBD8G_ERR_BAD_ARG;
+            if (cudaMemcpyAsync(output, input, r.elem_bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return RSBD8G_ERR_CUDA;
+            return cudaStreamSynchronize(s) == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+        }
+        return RSBD8G_OK;
+    }
+    if (!input || (!inplace && (!output || input == output))) return RSBD8G_ERR_BAD_ARG;
+    const Layout L = layout_for(r, count);
+    const size_t buf_bytes = (size_t(count) * r.elem_bytes + 255) & ~size_t(255);
+    void *mem = nullptr;
+    if (cudaMallocAsync(&mem, L.total + buf_bytes, s) != cudaSuccess || !mem) {
+        cudaGetLastError();
+        return RSBD8G_ERR_NO_MEMORY;
+    }
+    unsigned char *scratch = static_cast<unsigned char *>(mem);
+    void *buffer = scratch + L.total;
+    st = enqueue_sort(r, count, scratch, L.total, input, inplace ? nullptr : output, buffer, inplace, false, s);
+    rsbd8g_status dev = RSBD8G_OK;
+    if (st == RSBD8G_OK) dev = read_device_status(scratch, s, false);
+    cudaFreeAsync(mem, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && st == RSBD8G_OK) st = RSBD8G_ERR_CUDA;
+    return st != RSBD8G_OK ? st : dev;
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy(const rsbd8g_desc *desc, size_t count, const void *input, void *output,
+                                              rsbd8g_stream stream) {
+    return sort_alloc(desc, count, input, output, false, stream);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsort(const rsbd8g_desc *desc, size_t count, void *input, rsbd8g_stream stream) {
+    return sort_alloc(desc, count, input, nullptr, true, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// rsbd8g_device.cuh - device code of the GB300 stable LSD radix sort.
+//
+// Sorting semantics follow Radixsortbidi8.hpp (namespace rsbd8):
+//   * the filtered sort key K(b) of each of the 8 filter combinations:
+//     filterinput (Radixsortbidi8.hpp:10006-10027) plus the virtual MSB flip of the
+//     signed/floating-point modes and the virtual LSB flip of tiered absolute
+//     floating point done by the offsets generators (Radixsortbidi8.hpp:11629-11806);
+//   * the up-front histogram of every digit in one read of the keys
+//     (radixsortnoallocmultiinitmt, Radixsortbidi8.hpp:28919) and the pass-skip test
+//     "one bucket holds every key" (generateoffsets*, Radixsortbidi8.hpp:12238-12440);
+//   * one stable scatter per surviving digit that stores the original key bits
+//     (radixsortnoallocmultisortmain, Radixsortbidi8.hpp:31782-31982).
+// The GPU uses 8-bit digits throughout (the reference uses 11-bit digits for 32/64-bit
+// keys); a stable LSD sort's output depends only on the key order, so the result is
+// identical.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rsbd8g {
+
+constexpr int kRadixBits = 8;
+constexpr int kBuckets = 1 << kRadixBits;
+constexpr int kMaxPasses = 8;
+
+// device status bits (Control::error)
+enum : uint32_t { kDevTimeout = 1u, kDevFault = 2u };
+
+// look-back status word states (top two bits)
+enum : uint32_t { kStInvalid = 0u, kStAggregate = 1u, kStInclusive = 2u };
+
+// copy step after the scatter passes (Control::copy_mode)
+enum : uint32_t { kCopyNone = 0u, kCopyPlain = 1u, kCopyReversed = 2u, kReverseInPlace = 3u };
+
+struct Filter {
+    uint32_t absv, sign, fltp, desc;
+};
+
+struct PassPlan {
+    const void *src_keys;
+    void *dst_keys;        // may be null on the last indirect pass (keys are dropped)
+    const void *src_vals;  // indirect: object pointers
+    void *dst_vals;
+    uint32_t active;
+    uint32_t reverse;      // read the source back to front (isrevorder, first surviving pass)
+    uint32_t pad0, pad1;
+};
+
+struct Control {
+    uint32_t error;
+    uint32_t abort;
+    uint32_t tile_counter[kMaxPasses];
+    uint32_t active_passes;
+    uint32_t copy_mode;
+    const void *copy_src;
+    void *copy_dst;
+    uint64_t copy_elem_bytes;
+    uint32_t stall_tile;   // diagnostics: this tile never publishes (0xFFFFFFFF = off)
+    uint32_t pad;
+    uint64_t spin_limit_ns;
+    PassPlan plan[kMaxPasses];
+};
+static_assert(sizeof(Control) <= 1024, "control block must fit its slot");
+
+// ---- key filter -----------------------------------------------------------------------
+
+// K(b): transform raw key bits into an unsigned key whose ascending order is the
+// reference's order for the resolved mode; descending sorts use the complement.
+template <typename U>
+__device__ __forceinline__ U sortkey(U b, const Filter &f) {
+    constexpr int W = int(sizeof(U)) * 8;
+    const U sb = U(U(1) << (W - 1));
+    const U s = (b & sb) ? U(~U(0)) : U(0);   // sign mask
+    const U m = U(b & U(~sb));
+    U k;
+    if (f.absv != f.fltp) {
+        if (f.absv) k = f.sign ? U(U(b + s) ^ s) : U(U(b << 1) ^ s);      // abs signed / tiered abs signed
+        else k = f.sign ? U(U(U(m + s) ^ s) ^ sb) : U(m ^ s);              // float (+MSB flip) / inside-out float
+    } else if (f.absv) {
+        k = f.sign ? m : U(U(U(b << 1) | U(b >> (W - 1))) ^ U(1));        // abs float / tiered abs float
+    } else {
+        k = f.sign ? U(b ^ sb) : b;                                         // signed (MSB flip) / unsigned
+    }
+    return f.desc ? U(~k) : k;
+}
+
+template <typename U>
+__device__ __forceinline__ uint32_t digit_of(U k, int pass) {
+    return uint32_t(k >> (pass * kRadixBits)) & (kBuckets - 1);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(uint64_t *p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// status word helpers: state in the top two bits, count below
+template <typename S> struct StatusWord;
+template <> struct StatusWord<uint32_t> {
+    static constexpr int kShift = 30;
+    __device__ static uint32_t make(uint32_t st, uint64_t v) { return (st << kShift) | uint32_t(v); }
+    __device__ static uint32_t state(uint32_t w) { return w >> kShift; }
+    __device__ static uint64_t value(uint32_t w) { return w & ((1u << kShift) - 1u); }
+};
+template <> struct StatusWord<uint64_t> {
+    static constexpr int kShift = 62;
+    __device__ static uint64_t make(uint32_t st, uint64_t v) { return (uint64_t(st) << kShift) | v; }
+    __device__ static uint32_t state(uint64_t w) { return uint32_t(w >> kShift); }
+    __device__ static uint64_t value(uint64_t w) { return w & ((uint64_t(1) << kShift) - 1u); }
+};
+
+// load the raw bits of a key through an object pointer (unaligned members allowed)
+template <typename U>
+__device__ __forceinline__ U load_member(const unsigned char *p) {
+    if ((reinterpret_cast<uintptr_t>(p) & (sizeof(U) - 1)) == 0) return *reinterpret_cast<const U *>(p);
+    U v = 0;
+#pragma unroll
+    for (int i = 0; i < int(sizeof(U)); ++i) v |= U(U(p[i]) << (8 * i));
+    return v;
+}
+
+__device__ __forceinline__ const unsigned char *load_ptr(const unsigned char *p) {
+    if ((reinterpret_cast<uintptr_t>(p) & 7u) == 0) return *reinterpret_cast<const unsigned char *const *>(p);
+    uint64_t v = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v |= uint64_t(p[i]) << (8 * i);
+    return reinterpret_cast<const unsigned char *>(v);
+}
+
+}  // namespace rsbd8g

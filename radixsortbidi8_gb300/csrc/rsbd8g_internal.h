@@ -1,0 +1,37 @@
+// rsbd8g_internal.h - shared host-side declarations of the GB300 radix sort library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "rsbd8g.h"
+#include "rsbd8g_device.cuh"
+
+namespace rsbd8g {
+
+// a descriptor after the reference's compile-time mode resolution
+struct Resolved {
+    Filter f;
+    uint32_t rev;         // effective isrevorder
+    uint32_t key_bytes;   // 1, 2, 4, 8
+    uint32_t elem_bytes;  // bytes per array element (key bytes, or 8 for object pointers)
+    uint32_t indirect;    // RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2
+    uint32_t flags;
+    int64_t off1, off2;
+};
+
+// byte offsets of the parts of a scratch area
+struct Layout {
+    size_t ctrl, ghist, bstart, status, status_pass_bytes, zero_bytes, keys_a, keys_b, total;
+    uint32_t num_tiles;
+    bool wide_status;
+};
+
+rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
+Layout layout_for(const Resolved &r, uint64_t n);
+rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
+                           void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);
+rsbd8g_status read_device_status(void *scratch, cudaStream_t s, bool clear);
+
+}  // namespace rsbd8g

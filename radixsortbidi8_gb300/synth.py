@@ -1,0 +1,177 @@
+"""Seeded synthetic workloads of the benchmark configurations (deterministic, counter-based).
+
+Every value is a function of (seed, index) through splitmix64, so the same call gives
+the same data on any host; the torch variants compute the identical integer stream on
+the GPU for the large configurations (floating-point transforms such as Box-Muller may
+differ in the last bit between numpy and torch, which no test relies on).
+
+Workloads (the reference benchmarks random bit patterns only; these stand in for the
+configurations it is measured on):
+  * uniform bits of any 1/2/4/8-byte key type;
+  * uint32 with only the low 12 bits random (exercises the pass-skip test);
+  * float32/float64 N(0, sigma) with 1% -0.0, 0.5% +-inf and 0.1% NaN (half 0x7FC00000-style
+    positive quiet NaN, half negative);
+  * int64 uniform over the full signed range;
+  * 24-byte records {u64 id, f64 key, u32 tag, u32 pad}, key = lognormal(0, 2) x random sign,
+    10% of the records copy the key of an earlier random record;
+  * log-uniform segment lengths; Poisson arrival times.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+M1 = np.uint64(0xBF58476D1CE4E5B9)
+M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, offset: int = 0, stream: int = 0) -> np.ndarray:
+    """n uint64 values: splitmix64 of the counters offset..offset+n-1 (stream selects a sub-sequence)."""
+    with np.errstate(over="ignore"):
+        base = np.uint64((seed * 0x632BE59BD9B4E019 + stream * 0x8CB92BA72F3D8DD7) & 0xFFFFFFFFFFFFFFFF)
+        z = (np.arange(offset, offset + n, dtype=np.uint64) + np.uint64(1)) * GOLDEN + base
+        z = (z ^ (z >> np.uint64(30))) * M1
+        z = (z ^ (z >> np.uint64(27))) * M2
+        return z ^ (z >> np.uint64(31))
+
+
+def unit_interval(bits: np.ndarray) -> np.ndarray:
+    """uint64 -> float64 in (0, 1]."""
+    return ((bits >> np.uint64(11)).astype(np.float64) + 1.0) * (1.0 / 9007199254740992.0)
+
+
+def uniform_bits(seed: int, n: int, dtype) -> np.ndarray:
+    dt = np.dtype(dtype)
+    ut = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[dt.itemsize]
+    return splitmix64(seed, n).astype(ut).view(dt)
+
+
+def low_bits_u32(seed: int, n: int, bits: int = 12) -> np.ndarray:
+    return (splitmix64(seed, n) & np.uint64((1 << bits) - 1)).astype(np.uint32)
+
+
+def normal(seed: int, n: int, stream: int = 0) -> np.ndarray:
+    u1 = unit_interval(splitmix64(seed, n, stream=2 * stream + 1))
+    u2 = unit_interval(splitmix64(seed, n, stream=2 * stream + 2))
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def float_specials(seed: int, n: int, dtype=np.float32, sigma: float = 1e3) -> np.ndarray:
+    """N(0, sigma) with 1% -0.0, 0.5% +-inf (half each sign), 0.1% NaN (half each sign)."""
+    dt = np.dtype(dtype)
+    x = (normal(seed, n) * sigma).astype(dt)
+    r = unit_interval(splitmix64(seed, n, stream=7))
+    x[r <= 0.01] = -0.0
+    inf = (r > 0.01) & (r <= 0.015)
+    x[inf & (r <= 0.0125)] = np.inf
+    x[inf & (r > 0.0125)] = -np.inf
+    nan = (r > 0.015) & (r <= 0.016)
+    ut = {4: np.uint32, 8: np.uint64}[dt.itemsize]
+    qnan = {4: 0x7FC00000, 8: 0x7FF8000000000000}[dt.itemsize]
+    sbit = {4: 0x80000000, 8: 0x8000000000000000}[dt.itemsize]
+    bits = x.view(ut)
+    bits[nan & (r <= 0.0155)] = ut(qnan)
+    bits[nan & (r > 0.0155)] = ut(qnan | sbit)
+    return x
+
+
+def records24(seed: int, n: int) -> np.ndarray:
+    """24-byte records {u64 id, f64 key, u32 tag, u32 pad}; key = lognormal(0, 2) x random sign,
+    10% duplicate the key of an earlier random record."""
+    rec = np.zeros(n, dtype=[("id", "<u8"), ("key", "<f8"), ("tag", "<u4"), ("pad", "<u4")])
+    rec["id"] = np.arange(n, dtype=np.uint64)
+    key = np.exp(2.0 * normal(seed, n))
+    sgn = (splitmix64(seed, n, stream=11) & np.uint64(1)).astype(bool)
+    key = np.where(sgn, -key, key)
+    dup = unit_interval(splitmix64(seed, n, stream=12)) <= 0.1
+    dup[0] = False
+    src = (unit_interval(splitmix64(seed, n, stream=13)) * np.arange(n)).astype(np.int64)
+    src = np.minimum(src, np.maximum(np.arange(n) - 1, 0))
+    # a duplicate copies the final key of its source, which may itself be a duplicate
+    root = np.where(dup, src, np.arange(n))
+    while True:
+        chain = dup[root]
+        if not chain.any():
+            break
+        root[chain] = src[root[chain]]
+    rec["key"] = key[root]
+    rec["tag"] = (splitmix64(seed, n, stream=14) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    return rec
+
+
+def log_uniform_lengths(seed: int, count: int, lo: int, hi: int) -> np.ndarray:
+    u = unit_interval(splitmix64(seed, count, stream=21))
+    return np.minimum(np.floor(np.exp(u * np.log(hi / lo)) * lo), hi).astype(np.int64)
+
+
+def poisson_arrivals(seed: int, rate: float, duration: float) -> np.ndarray:
+    """Arrival times (s) of a Poisson process of `rate` per second over `duration` seconds."""
+    est = int(rate * duration * 1.2 + 100)
+    gaps = -np.log(unit_interval(splitmix64(seed, est, stream=31))) / rate
+    t = np.cumsum(gaps)
+    return t[t < duration]
+
+
+# ---- GPU (torch) versions of the integer stream, for the large configurations -------------
+
+def splitmix64_torch(seed: int, n: int, device="cuda", offset: int = 0, stream: int = 0):
+    """The splitmix64 stream of splitmix64(), computed on the device as int64 (same bits)."""
+    import torch
+
+    def s64(v):
+        v &= 0xFFFFFFFFFFFFFFFF
+        return v - (1 << 64) if v >= (1 << 63) else v
+
+    base = s64(seed * 0x632BE59BD9B4E019 + stream * 0x8CB92BA72F3D8DD7)
+    z = torch.arange(offset + 1, offset + n + 1, dtype=torch.int64, device=device)
+    z.mul_(s64(0x9E3779B97F4A7C15)).add_(base)
+
+    def lsr(x, k):
+        return (x >> k) & ((1 << (64 - k)) - 1)
+
+    z = (z ^ lsr(z, 30)) * s64(0xBF58476D1CE4E5B9)
+    z = (z ^ lsr(z, 27)) * s64(0x94D049BB133111EB)
+    return z ^ lsr(z, 31)
+
+
+def uniform_bits_torch(seed: int, n: int, key_bytes: int, device="cuda"):
+    """Uniform random key bits as a signed torch tensor of key_bytes width."""
+    import torch
+    z = splitmix64_torch(seed, n, device)
+    if key_bytes == 8:
+        return z
+    t = {1: torch.int8, 2: torch.int16, 4: torch.int32}[key_bytes]
+    mask = (1 << (8 * key_bytes)) - 1
+    half = 1 << (8 * key_bytes - 1)
+    v = z & mask
+    return torch.where(v >= half, v - (1 << (8 * key_bytes)), v).to(t)
+
+
+def low_bits_u32_torch(seed: int, n: int, bits: int = 12, device="cuda"):
+    import torch
+    return (splitmix64_torch(seed, n, device) & ((1 << bits) - 1)).to(torch.int32)
+
+
+def float_specials_torch(seed: int, n: int, key_bytes: int = 4, sigma: float = 1e3, device="cuda"):
+    """float_specials() computed on the device; returns the key bits as int32/int64."""
+    import torch
+
+    def unit(z):
+        return (((z >> 11) & ((1 << 53) - 1)).to(torch.float64) + 1.0) * (1.0 / 9007199254740992.0)
+
+    u1 = unit(splitmix64_torch(seed, n, device, stream=1))
+    u2 = unit(splitmix64_torch(seed, n, device, stream=2))
+    x = torch.sqrt(-2.0 * torch.log(u1)) * torch.cos(2.0 * np.pi * u2) * sigma
+    del u1, u2
+    r = unit(splitmix64_torch(seed, n, device, stream=7))
+    if key_bytes == 4:
+        x = x.to(torch.float32)
+    x[r <= 0.01] = -0.0
+    x[(r > 0.01) & (r <= 0.0125)] = float("inf")
+    x[(r > 0.0125) & (r <= 0.015)] = float("-inf")
+    bits = x.view(torch.int32 if key_bytes == 4 else torch.int64)
+    qnan = 0x7FC00000 if key_bytes == 4 else 0x7FF8000000000000
+    nqnan = (0x7FC00000 | 0x80000000) - (1 << 32) if key_bytes == 4 else (0x7FF8000000000000 | (1 << 63)) - (1 << 64)
+    bits[(r > 0.015) & (r <= 0.0155)] = qnan
+    bits[(r > 0.0155) & (r <= 0.016)] = nqnan
+    return bits

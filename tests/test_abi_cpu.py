@@ -1,0 +1,83 @@
+"""The C-ABI library without a GPU: it loads, exports every function include/*.h declares,
+sizes scratch, and rejects bad descriptors before touching the device."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import radixsortbidi8_gb300 as rs
+from radixsortbidi8_gb300 import api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        names |= set(re.findall(r"RSBD8G_API\s+[\w\s\*]+?\b(rsbd8g_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("rsbd8g_radixsortcopy", "rsbd8g_radixsort", "rsbd8g_radixsortcopynoalloc",
+                 "rsbd8g_radixsortnoalloc", "rsbd8g_scratch_bytes"):
+        assert must in names
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    L = rs.lib()
+    for name in declared_symbols():
+        assert hasattr(L, name), name
+    assert L.rsbd8g_version() >= 100
+    assert L.rsbd8g_status_string(4) == b"device-side wait timed out"
+
+
+def test_library_is_sm103a_only():
+    out = os.popen(f"cuobjdump --list-elf {api.library_path()} 2>/dev/null").read()
+    if not out:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out
+
+
+def test_scratch_sizes():
+    s20 = rs.scratch_bytes(np.uint32, 1 << 20)
+    s28 = rs.scratch_bytes(np.uint32, 1 << 28)
+    assert 0 < s20 < s28
+    # look-back state: one 4-byte word per (tile, bucket, digit) below 2^30 keys, 8 bytes above
+    assert s28 < 200 << 20
+    assert rs.scratch_bytes(np.uint64, 1 << 30) > 2 * rs.scratch_bytes(np.uint64, (1 << 30) - 1) * 0.9
+    # indirection also holds the gathered keys twice
+    assert rs.scratch_bytes(np.float64, 1 << 20, indirection=api.MEMBER, offset1=8) > 2 * 8 * (1 << 20)
+
+
+def test_bad_descriptors_rejected_without_a_device():
+    L = rs.lib()
+    out = ctypes.c_size_t()
+    for kb, kind, mode, d in [(3, 0, 64, 0), (4, 0, 9, 0), (4, 0, 64, 4), (2, 2, 64, 0), (4, 7, 64, 0)]:
+        desc = api.Desc(kb, kind, mode, d, 0, 0, 0, 0)
+        assert L.rsbd8g_scratch_bytes(ctypes.byref(desc), 10, ctypes.byref(out)) == api.ERR_BAD_ARG
+        assert L.rsbd8g_radixsortcopy(ctypes.byref(desc), 10, 1, 2, None) == api.ERR_BAD_ARG
+    good = api.make_desc(np.uint32)
+    assert L.rsbd8g_scratch_bytes(ctypes.byref(good), 1 << 41, ctypes.byref(out)) == api.ERR_TOO_LARGE
+    # count 0 is sorted already (the reference returns true without touching the arrays)
+    assert L.rsbd8g_radixsortcopy(ctypes.byref(good), 0, None, None, None) == api.OK
+    assert L.rsbd8g_radixsortcopy(ctypes.byref(good), 5, 4096, 4096, None) == api.ERR_BAD_ARG   # aliasing
+
+
+def test_key_kinds_follow_std_type_traits():
+    assert rs.key_kind(np.uint16) == (0, 2)
+    assert rs.key_kind(np.int64) == (1, 8)
+    assert rs.key_kind(np.float32) == (2, 4)
+    assert rs.key_kind(np.bool_) == (0, 1)
+
+
+def test_no_cpu_fallback_in_product_path():
+    """The product package never imports the oracle."""
+    for f in glob.glob(os.path.join(ROOT, "radixsortbidi8_gb300", "**", "*.py"), recursive=True):
+        src = open(f).read()
+        assert not re.search(r"^\s*(from|import)\s+oracle", src, re.M), f

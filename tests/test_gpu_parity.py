@@ -1,0 +1,278 @@
+"""GPU parity: the sm_103a sort through the C ABI against the oracle, bit for bit.
+
+Every case sorts the same seeded input on the GPU and with the oracle's C restatement
+(oracle/rsbd8_oracle.c) and compares the bytes: keys, tie order (stability, -0.0/+0.0,
+NaN placement) and, for indirection, the exact pointer order.
+"""
+import numpy as np
+import pytest
+
+from conftest import empty_dev, from_dev, same_bits, to_dev
+from oracle import oracle as O
+from radixsortbidi8_gb300 import synth as S
+
+pytestmark = pytest.mark.gpu
+
+DIRS = ["ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"]
+TYPES = [np.uint8, np.int8, np.uint16, np.int16, np.uint32, np.int32, np.float32,
+         np.uint64, np.int64, np.float64]
+EDGE_SIZES = [2, 3, 31, 32, 33, 255, 256, 257, 4095, 4097, 8191, 8192, 8193, 16385, 65543]
+ALL_MODES = ["native", "nativeabs", "nativetieredabs", "forceunsigned", "forcesigned", "forceabssigned",
+             "forcefloatingp", "forceabsfloatingp", "specialfloatingp", "forcetieredabsfloatingp",
+             "forcetieredabssigned"]
+
+
+def R():
+    import radixsortbidi8_gb300 as rs
+    return rs
+
+
+def gpu_copy(a, mode="native", direction="ascfwdorder"):
+    inp = to_dev(a)
+    out = empty_dev(a.size, a.dtype)
+    assert R().radixsortcopy(inp, out, direction, mode, key_dtype=a.dtype)
+    # the input must be untouched
+    assert same_bits(from_dev(inp, a.dtype), a)
+    return from_dev(out, a.dtype)
+
+
+def gpu_inplace(a, mode="native", direction="ascfwdorder"):
+    t = to_dev(a)
+    assert R().radixsort(t, direction, mode, key_dtype=a.dtype)
+    return from_dev(t, a.dtype)
+
+
+def mixed_input(dt, n, seed):
+    """uniform bits, with specials for floats and duplicates for everyone"""
+    dt = np.dtype(dt)
+    if dt.kind == "f":
+        a = S.float_specials(seed, n, dt)
+    else:
+        a = S.uniform_bits(seed, n, dt)
+    if n > 8:
+        a[:: 7] = a[3]      # duplicates
+    return a
+
+
+@pytest.mark.parametrize("dt", TYPES, ids=lambda t: np.dtype(t).name)
+@pytest.mark.parametrize("direction", DIRS)
+def test_native_modes_all_types(dt, direction):
+    for n in (0, 1, 2, 1000, 40009):
+        a = mixed_input(dt, n, 100 + n)
+        assert same_bits(gpu_copy(a, "native", direction), O.sortcopy(a, "native", direction)), (n,)
+
+
+@pytest.mark.parametrize("mode", ALL_MODES)
+@pytest.mark.parametrize("dt", [np.int16, np.int32, np.float32, np.int64, np.float64], ids=lambda t: np.dtype(t).name)
+def test_every_mode_and_direction(mode, dt):
+    if np.dtype(dt).itemsize == 2 and mode in ("forcefloatingp", "forceabsfloatingp",
+                                             "specialfloatingp", "forcetieredabsfloatingp"):
+        pass  # forced float modes on 16-bit keys are still defined (the mode bits pick the filter)
+    a = mixed_input(dt, 30011, 7)
+    for d in DIRS:
+        assert same_bits(gpu_copy(a, mode, d), O.sortcopy(a, mode, d)), d
+
+
+@pytest.mark.parametrize("n", EDGE_SIZES)
+def test_edge_sizes_u32_f32(n):
+    for dt, mode, d in [(np.uint32, "native", "ascfwdorder"), (np.float32, "native", "dscrevorder"),
+                        (np.float32, "nativeabs", "dscfwdorder"), (np.int64, "native", "ascfwdorder")]:
+        a = mixed_input(dt, n, n)
+        assert same_bits(gpu_copy(a, mode, d), O.sortcopy(a, mode, d)), (dt, mode, d)
+
+
+def test_pass_skip_low12_and_all_equal():
+    # only the low 12 bits random: digits 2 and 3 skipped
+    a = S.low_bits_u32(4, 1 << 20)
+    assert O.skipmask(a, digit_bits=8) == 0b1100
+    assert same_bits(gpu_copy(a), O.sortcopy(a))
+    # every digit skipped: plain copy, reversed copy under isrevorder, in place too
+    for dt, mode in [(np.uint32, "native"), (np.float32, "native"), (np.float32, "nativeabs")]:
+        b = np.full(50000, 3, dtype=dt)
+        if dt == np.float32:
+            # -0.0 and +0.0 share one sort key; under the absolute filter so do -2.5 and 2.5
+            b = np.where(np.arange(b.size) % 3 == 0, np.float32(-0.0), np.float32(0.0))
+            if mode == "nativeabs":
+                b = np.where(np.arange(b.size) % 3 == 0, np.float32(-2.5), np.float32(2.5))
+        for d in DIRS:
+            assert same_bits(gpu_copy(b, mode, d), O.sortcopy(b, mode, d)), (dt, mode, d)
+            assert same_bits(gpu_inplace(b, mode, d), O.sortcopy(b, mode, d)), (dt, mode, d)
+
+
+def test_two_keys_sorted_reversed():
+    for a in (np.tile(np.array([5, 1], np.uint32), 30000), np.arange(100000, dtype=np.uint32),
+              np.arange(100000, dtype=np.int32)[::-1].copy(), np.arange(-50000, 50000, dtype=np.int64)):
+        for d in DIRS:
+            assert same_bits(gpu_copy(a, "native", d), O.sortcopy(a, "native", d))
+
+
+def test_float_lattice_and_int_extremes():
+    f = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, -np.nan, 1e-45, -1e-45, 1.0, -1.0,
+                  3.4028235e38, -3.4028235e38, 1.1754944e-38, -1.1754944e-38], dtype=np.float32)
+    f = np.tile(f, 997)
+    f.view(np.uint32)[::13] ^= 0x00000001  # NaN payload / subnormal variants
+    for mode in ALL_MODES:
+        for d in DIRS:
+            assert same_bits(gpu_copy(f, mode, d), O.sortcopy(f, mode, d)), (mode, d)
+    i = np.tile(np.array([0, -1, 1, -2, 2, np.iinfo(np.int32).min, np.iinfo(np.int32).max, -3, 5, -5],
+                         np.int32), 3001)
+    for mode in ALL_MODES:
+        for d in DIRS:
+            assert same_bits(gpu_copy(i, mode, d), O.sortcopy(i, mode, d)), (mode, d)
+
+
+def test_inplace_and_noalloc_forms():
+    import torch
+    rs = R()
+    for dt, mode, d in [(np.uint32, "native", "ascfwdorder"), (np.float64, "native", "dscrevorder"),
+                        (np.int16, "nativetieredabs", "ascfwdorder"), (np.float32, "nativeabs", "ascrevorder")]:
+        for n in (5, 8193, 70001):
+            a = mixed_input(dt, n, n + 1)
+            want = O.sortcopy(a, mode, d)
+            assert same_bits(gpu_inplace(a, mode, d), want)
+            nbytes = rs.scratch_bytes(dt, n, d, mode)
+            scratch = torch.full((nbytes,), 0x5A, dtype=torch.uint8, device="cuda")  # garbage content
+            inp, out, buf = to_dev(a), empty_dev(n, dt), empty_dev(n, dt)
+            rs.radixsortcopynoalloc(inp, out, buf, scratch, d, mode, key_dtype=dt)
+            assert rs.scratch_status(scratch) == 0
+            assert same_bits(from_dev(out, dt), want)
+            for mtb in (False, True):
+                x, b2 = to_dev(a), empty_dev(n, dt)
+                rs.radixsortnoalloc(x, b2, scratch, mtb, d, mode, key_dtype=dt)
+                assert rs.scratch_status(scratch) == 0
+                assert same_bits(from_dev(b2 if mtb else x, dt), want), (dt, n, mtb)
+
+
+def test_graph_capture_of_noalloc():
+    import torch
+    rs = R()
+    n = 100003
+    a = mixed_input(np.float32, n, 77)
+    inp, out, buf = to_dev(a), empty_dev(n, np.float32), empty_dev(n, np.float32)
+    scratch = torch.empty(rs.scratch_bytes(np.float32, n, "dscfwdorder"), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        rs.radixsortcopynoalloc(inp, out, buf, scratch, "dscfwdorder", key_dtype=np.float32, stream=s)
+        s.synchronize()
+        with torch.cuda.graph(g, stream=s):
+            rs.radixsortcopynoalloc(inp, out, buf, scratch, "dscfwdorder", key_dtype=np.float32, stream=s)
+    want = O.sortcopy(a, "native", "dscfwdorder")
+    for seed in (1, 2):
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert same_bits(from_dev(out, np.float32), want)
+    # new input bytes in the same buffers
+    b = mixed_input(np.float32, n, 78)
+    inp.copy_(to_dev(b))
+    g.replay()
+    torch.cuda.synchronize()
+    assert same_bits(from_dev(out, np.float32), O.sortcopy(b, "native", "dscfwdorder"))
+
+
+def test_lookback_timeout_is_reported_and_device_recovers():
+    """A tile that never publishes makes its successors' bounded waits run out: the call
+    reports a timeout instead of hanging, and the device keeps working."""
+    rs = R()
+    a = S.uniform_bits(9, 8192 * 6, np.uint32)
+    inp, out = to_dev(a), empty_dev(a.size, np.uint32)
+    with pytest.raises(rs.RSBD8GError) as e:
+        rs.radixsortcopy(inp, out, key_dtype=np.uint32, flags=1)
+    assert e.value.status == 4
+    assert same_bits(gpu_copy(a), O.sortcopy(a))
+
+
+def test_bad_arguments_rejected():
+    import torch
+    rs = R()
+    a = to_dev(np.arange(100, dtype=np.uint32))
+    with pytest.raises(rs.RSBD8GError):
+        rs.radixsortcopy(a, a, key_dtype=np.uint32)          # aliasing
+    with pytest.raises(rs.RSBD8GError):
+        rs.radixsortcopy(a, empty_dev(100, np.uint32), mode=9, key_dtype=np.uint32)
+    small = torch.empty(16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(rs.RSBD8GError):
+        rs.radixsortcopynoalloc(a, empty_dev(100, np.uint32), empty_dev(100, np.uint32), small, key_dtype=np.uint32)
+
+
+@pytest.mark.parametrize("n", [2 ** 20, 2 ** 20 + 12345])
+def test_config1_u32_uniform_bit_exact(n):
+    a = S.uniform_bits(0x5EED0001, n, np.uint32)
+    got = gpu_copy(a)
+    assert same_bits(got, O.sortcopy(a, threads=8))
+    assert same_bits(got, np.sort(a, kind="stable"))
+
+
+# ---- indirection ----------------------------------------------------------------------------
+
+def _records_dev(rec: np.ndarray):
+    import torch
+    raw = torch.from_numpy(rec.view(np.uint8).copy()).cuda()
+    return raw, raw.data_ptr()
+
+
+@pytest.mark.parametrize("direction", DIRS)
+def test_indirect_records_f64_bit_exact(direction):
+    import torch
+    rs = R()
+    n = 200003
+    rec = S.records24(0x5EED0003, n)
+    raw, base = _records_dev(rec)
+    ptrs = torch.arange(n, dtype=torch.int64, device="cuda") * 24 + base
+    out = torch.empty_like(ptrs)
+    assert rs.radixsortcopy_member(ptrs, out, np.float64, 8, direction)
+    idx = (out.cpu().numpy() - base) // 24
+    # oracle on host copies of the same records
+    host_ptrs = np.uint64(rec.ctypes.data) + np.arange(n, dtype=np.uint64) * np.uint64(24)
+    want = (O.sortcopy_indirect(host_ptrs, np.float64, 8, "native", direction, threads=8)
+            - np.uint64(rec.ctypes.data)) // np.uint64(24)
+    assert np.array_equal(idx, want.astype(np.int64))
+    assert np.array_equal(idx, O.numpy_sort_indices(rec["key"].copy(), "native", direction))
+
+
+@pytest.mark.parametrize("kt,off", [(np.uint32, 8), (np.float32, 12), (np.int64, 0), (np.uint16, 16),
+                                    (np.int32, 9), (np.uint64, 9), (np.float64, 17)])
+def test_indirect_key_types_and_unaligned_offsets(kt, off):
+    import torch
+    rs = R()
+    n, size = 50021, 25          # packed 25-byte objects: offsets 9 and 17 are unaligned
+    bytes_ = S.uniform_bits(31, n * size, np.uint8)
+    keys = mixed_input(kt, n, 5)
+    kb = np.dtype(kt).itemsize
+    obj = bytes_.reshape(n, size).copy()
+    obj[:, off:off + kb] = keys.view(np.uint8).reshape(n, kb)
+    raw = torch.from_numpy(obj.reshape(-1).copy()).cuda()
+    base = raw.data_ptr()
+    perm = np.argsort(S.splitmix64(3, n))  # shuffled pointer order
+    ptrs = torch.from_numpy((perm * size).astype(np.int64)).cuda() + base
+    for d in DIRS:
+        out = torch.empty_like(ptrs)
+        assert rs.radixsortcopy_member(ptrs, out, kt, off, d)
+        idx = (out.cpu().numpy() - base) // size
+        hobj = obj.reshape(-1)
+        hp = np.uint64(hobj.ctypes.data) + (perm * size).astype(np.uint64)
+        want = (O.sortcopy_indirect(hp, kt, off, "native", d) - np.uint64(hobj.ctypes.data)) // np.uint64(size)
+        assert np.array_equal(idx, want.astype(np.int64)), d
+
+
+def test_indirect_second_level_and_inplace():
+    import torch
+    rs = R()
+    n = 30011
+    keys = mixed_input(np.float32, n, 12)
+    kdev = to_dev(keys)                                   # the keys, 4 bytes each
+    # first-level objects: 16 bytes {u64 pad, u64 pointer to a key}
+    holders = np.zeros((n, 2), dtype=np.uint64)
+    holders[:, 1] = np.uint64(kdev.data_ptr()) + np.arange(n, dtype=np.uint64) * np.uint64(4)
+    hdev = torch.from_numpy(holders.view(np.int64).reshape(-1).copy()).cuda()
+    ptrs = torch.arange(n, dtype=torch.int64, device="cuda") * 16 + hdev.data_ptr()
+    for d in DIRS:
+        out = torch.empty_like(ptrs)
+        assert rs.radixsortcopy_member(ptrs, out, np.float32, 8, d, offset2=0)
+        idx = (out.cpu().numpy() - hdev.data_ptr()) // 16
+        assert np.array_equal(idx, O.numpy_sort_indices(keys, "native", d)), d
+        # in place
+        p2 = ptrs.clone()
+        assert rs.radixsort_member(p2, np.float32, 8, d, offset2=0)
+        assert np.array_equal((p2.cpu().numpy() - hdev.data_ptr()) // 16, idx)

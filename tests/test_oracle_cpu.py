@@ -1,0 +1,179 @@
+"""The oracle, pinned: known answers of the reference's own tests, the reference-generated
+golden fixtures, the independent numpy restatement, and (where it was compiled here) the
+reference itself on sizes where its snapshot is sound.  CPU only."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from radixsortbidi8_gb300 import synth as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "ref_golden.json")
+DIRS = ["ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"]
+TYPES = [np.uint8, np.int8, np.uint16, np.int16, np.uint32, np.int32, np.float32, np.uint64, np.int64,
+         np.float64]
+ALL_MODES = ["native", "nativeabs", "nativetieredabs", "forceunsigned", "forcesigned", "forceabssigned",
+             "forcefloatingp", "forceabsfloatingp", "specialfloatingp", "forcetieredabsfloatingp",
+             "forcetieredabssigned"]
+
+
+def same(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+# ---- known answers of the reference's portable unit test (multiplatform/main.cpp) ----------
+
+def test_known_answer_u32_main_cpp_10_19():
+    a = np.array([18, 33, 21, 0, 5, 1, 13], np.uint32)          # multiplatform/main.cpp:10-19
+    assert O.sortcopy(a).tolist() == [0, 1, 5, 13, 18, 21, 33]
+
+
+def test_known_answer_enum8_main_cpp_182_198():
+    # single-byte enum cert_v_binencoding64: $0=0 $i=18 $q=26 $B=37 $E=40 $U=56 $_=63
+    tein = np.array([0, 37, 63, 18, 26, 56, 40], np.uint8)       # multiplatform/main.cpp:191
+    assert O.sortcopy(tein, "native", "dscrevorder").tolist() == [63, 56, 40, 37, 26, 18, 0]
+    assert O.sortcopy(tein, "native", "ascfwdorder").tolist() == [0, 18, 26, 37, 40, 56, 63]
+
+
+def test_known_answer_float_bits_main_cpp_201_205():
+    inm = np.array([8, 0, 3, 0x80000002, 3, 0x80000012, 0x80000002], np.uint32).view(np.float32)
+    out = O.sortcopy(inm).view(np.uint32)
+    assert out.tolist() == [0x80000012, 0x80000002, 0x80000002, 0, 3, 3, 8]
+
+
+def test_known_answer_float_pointer_ties_main_cpp_208_215():
+    # pointers into the sorted float array; ties (0x80000002 x2, 3 x2) are told apart by address
+    outm = np.array([0x80000012, 0x80000002, 0x80000002, 0, 3, 3, 8], np.uint32)
+    inim_idx = np.array([6, 3, 4, 1, 5, 0, 2])
+    base = np.uint64(outm.ctypes.data)
+    inim = base + inim_idx.astype(np.uint64) * np.uint64(4)
+    got = O.sortcopy_indirect(inim, np.float32, 0, "native", "dscrevorder")
+    want = inim[[0, 4, 2, 1, 6, 3, 5]]                           # main.cpp:212
+    assert np.array_equal(got, want)
+    got = O.sortcopy_indirect(inim, np.float32, 0, "native", "ascfwdorder")
+    vals = outm[((got - base) // np.uint64(4)).astype(np.int64)]
+    assert vals.tolist() == [0x80000012, 0x80000002, 0x80000002, 0, 3, 3, 8]
+
+
+def test_known_answer_float_specials_order():
+    # -NaN < -inf < -1 < -0 == +0 < 1 < +inf < +NaN, ties in input order
+    a = np.array([1.0, -0.0, 0.0, -0.0, -1.0, np.nan, -np.nan, np.inf, -np.inf], np.float32)
+    a.view(np.uint32)[6] = 0xFFC00000
+    a.view(np.uint32)[5] = 0x7FC00000
+    got = O.sortcopy(a).view(np.uint32).tolist()
+    assert got == [0xFFC00000, 0xFF800000, 0xBF800000, 0x80000000, 0x00000000, 0x80000000,
+                   0x3F800000, 0x7F800000, 0x7FC00000]
+
+
+def test_known_answer_tiered_abs_signed():
+    a = np.array([0, -1, 1, -2, 2, 5, -5, np.iinfo(np.int32).min, np.iinfo(np.int32).max, -3], np.int32)
+    assert O.sortcopy(a, "nativetieredabs").tolist() == [0, -1, 1, -2, 2, -3, -5, 5, 2147483647, -2147483648]
+
+
+def test_sorting_mode_documented_orders():
+    """The orders the reference documents for the special modes (Radixsortbidi8.hpp:212-250)."""
+    z, nz, pinf, ninf, pnan, nnan = 0x0, 0x80000000, 0x7F800000, 0xFF800000, 0x7FC00000, 0xFFC00000
+    a = np.array([nnan, ninf, nz, z, pinf, pnan], np.uint32).view(np.float32)
+    # inside-out floating point: +0, +inf, +NaN, -NaN, -inf, -0
+    assert O.sortcopy(a, "specialfloatingp").view(np.uint32).tolist() == [z, pinf, pnan, nnan, ninf, nz]
+    # tiered absolute floating point: -0, +0, -inf, +inf, then NaNs
+    got = O.sortcopy(a, "forcetieredabsfloatingp").view(np.uint32).tolist()
+    assert got[:4] == [nz, z, ninf, pinf]
+    # inside-out signed integer (specialsigned = unsigned order): 0, max, min, -1
+    i = np.array([-1, np.iinfo(np.int16).min, np.iinfo(np.int16).max, 0], np.int16)
+    assert O.sortcopy(i, "specialsigned").tolist() == [0, 32767, -32768, -1]
+
+
+# ---- the two restatements agree -----------------------------------------------------------
+
+@pytest.mark.parametrize("dt", TYPES, ids=lambda t: np.dtype(t).name)
+def test_c_and_numpy_restatements_agree(dt):
+    for n in (0, 1, 2, 3, 257, 4099):
+        a = S.float_specials(n, n, dt) if np.dtype(dt).kind == "f" else S.uniform_bits(n, n, dt)
+        if n > 8:
+            a[::5] = a[2]
+        for mode in ALL_MODES:
+            if np.dtype(dt).itemsize < 4 and mode in ("nativeabs",):
+                pass
+            for d in DIRS:
+                c = O.sortcopy(a, mode, d, threads=3)
+                assert same(c, O.numpy_sortcopy(a, mode, d)), (n, mode, d)
+
+
+def test_multithreaded_oracle_matches_single_thread():
+    a = S.float_specials(5, 200003, np.float64)
+    for d in DIRS:
+        assert same(O.sortcopy(a, "native", d, threads=1), O.sortcopy(a, "native", d, threads=8))
+
+
+def test_indirect_oracle_matches_numpy():
+    rec = S.records24(3, 50000)
+    base = np.uint64(rec.ctypes.data)
+    ptrs = base + np.arange(rec.size, dtype=np.uint64) * np.uint64(24)
+    for d in DIRS:
+        got = (O.sortcopy_indirect(ptrs, np.float64, 8, "native", d, threads=4) - base) // np.uint64(24)
+        assert np.array_equal(got.astype(np.int64), O.numpy_sort_indices(rec["key"].copy(), "native", d))
+
+
+def test_pass_skip_mask():
+    assert O.skipmask(S.low_bits_u32(1, 1 << 16), digit_bits=8) == 0b1100
+    assert O.skipmask(np.full(100, 7, np.uint64), digit_bits=8) == 0xFF
+    assert O.skipmask(S.uniform_bits(2, 1 << 16, np.uint32), digit_bits=8) == 0
+
+
+# ---- golden fixtures generated by the reference itself -------------------------------------
+
+def _golden_cases():
+    if not os.path.exists(GOLDEN):
+        return []
+    with open(GOLDEN) as f:
+        return json.load(f)["cases"]
+
+
+def _oracle_case_bytes(c) -> bytes:
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import make_input
+    if c["form"] in ("indirect8", "member"):
+        n = c["n"]
+        if c["gen"] == "records":
+            buf = S.records24(c["seed"], n).view(np.uint8).reshape(n, 24).copy()
+        else:
+            keys = make_input("mixed", c["dtype"], n, c["seed"])
+            buf = np.zeros((n, 24), np.uint8)
+            kb = keys.dtype.itemsize
+            buf[:, 8:8 + kb] = keys.view(np.uint8).reshape(n, kb)
+        base = np.uint64(buf.ctypes.data)
+        ptrs = base + np.arange(n, dtype=np.uint64) * np.uint64(24)
+        out = O.sortcopy_indirect(ptrs, c["dtype"], 8, c["mode"], c["direction"], threads=8)
+        return ((out - base) // np.uint64(24)).astype(np.uint64).tobytes()
+    a = make_input(c["gen"], c["dtype"], c["n"], c["seed"])
+    return O.sortcopy(a, c["mode"], c["direction"], threads=8).tobytes()
+
+
+@pytest.mark.parametrize("case", [c for c in _golden_cases() if c["status"] == "ok"], ids=lambda c: str(c["id"]))
+def test_oracle_matches_reference_golden(case):
+    assert hashlib.sha256(_oracle_case_bytes(case)).hexdigest() == case["sha256"]
+
+
+def test_golden_fixture_present_and_mostly_sound():
+    cs = _golden_cases()
+    assert len(cs) > 100
+    ok = sum(c["status"] == "ok" for c in cs)
+    assert ok >= 0.8 * len(cs)
+
+
+# ---- the reference itself, live (only where it was compiled here) ---------------------------
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference adapter not built on this host")
+@pytest.mark.parametrize("dt", TYPES, ids=lambda t: np.dtype(t).name)
+def test_oracle_matches_reference_live_small(dt):
+    # single-threaded sizes of the reference (its multithreaded paths race at some sizes)
+    for n in (2, 3, 31, 256, 1000):
+        a = S.float_specials(n, n, dt) if np.dtype(dt).kind == "f" else S.uniform_bits(n, n, dt)
+        for d in DIRS:
+            assert same(O.ref_sortcopy(a, "native", d), O.sortcopy(a, "native", d)), (n, d)
