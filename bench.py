@@ -53,6 +53,8 @@ def parse_args():
     p.add_argument("--log2n", type=int, default=28, help="keys per array (2^log2n)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind"],
+                   help="profiling aid: sort only this one array --steps times and print its timings")
     return p.parse_args()
 
 
@@ -434,8 +436,54 @@ def reference_arm(args, rank: int, world: int) -> dict | None:
                     "compiled code does not travel to this host)"}
 
 
+def single_case(args) -> dict:
+    """One workload alone (for ncu captures of a small case): uniform uint32, int64, the float32
+    absolute descending array, the low-12-bit uint32 array, or the 24-byte record indirection."""
+    import numpy as np
+    import torch
+    import radixsortbidi8_gb300 as rs
+    from radixsortbidi8_gb300 import synth as S
+    dev = torch.device("cuda", 0)
+    n = 1 << args.log2n
+    stream = torch.cuda.current_stream()
+    if args.case == "f64ind":
+        rec = torch.empty(n * 24, dtype=torch.uint8, device=dev)
+        keys = S.float_specials_torch(SEEDS["f32"], n, 8, device=dev)
+        rec.view(torch.int64).view(n, 3)[:, 1] = keys
+        ptrs = torch.arange(n, dtype=torch.int64, device=dev) * 24 + rec.data_ptr()
+        out = torch.empty_like(ptrs)
+        run = lambda: rs.radixsortcopy_member(ptrs, out, np.float64, 8)
+    else:
+        kb, kdt, d, m, gen = {"u32": (4, np.uint32, "ascfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["u32"], n, 4, device=dev)),
+                              "i64": (8, np.int64, "ascfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["i64"], n, 8, device=dev)),
+                              "f32abs": (4, np.float32, "dscfwdorder", "nativeabs", lambda: S.float_specials_torch(SEEDS["f32"], n, 4, device=dev)),
+                              "u32low12": (4, np.uint32, "ascfwdorder", "native", lambda: S.low_bits_u32_torch(SEEDS["u32low12"], n, device=dev))}[args.case]
+        bits = gen()
+        out, buf = torch.empty_like(bits), torch.empty_like(bits)
+        scr = torch.empty(rs.scratch_bytes(kdt, n, d, m), dtype=torch.uint8, device=dev)
+        run = lambda: rs.radixsortcopynoalloc(bits, out, buf, scr, d, m, key_dtype=kdt, stream=stream)
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    rs.api.profile_enable(True)
+    for _ in range(args.steps):
+        run()
+    torch.cuda.synchronize()
+    rs.api.profile_enable(False)
+    recs = rs.api.profile_collect()
+    agg = {}
+    for r in recs:
+        agg.setdefault(r["kernel"], []).append(r["ms"])
+    return {"case": args.case, "n": n, "steps": args.steps,
+            "ms_per_sort": round(sum(r["ms"] for r in recs) / args.steps, 4),
+            "kernels": {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 4)} for k, v in agg.items()}}
+
+
 def main():
     args = parse_args()
+    if args.case:
+        print(json.dumps(single_case(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world > 1 and args.impl == "gb300":

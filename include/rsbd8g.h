@@ -73,8 +73,9 @@ enum {
     RSBD8G_DIRECT = 0,      /* the arrays hold the keys themselves */
     RSBD8G_MEMBER = 1,      /* the arrays hold object pointers; the key is at byte offset1 of each object
                                (member object pointer or type+offset form) */
-    RSBD8G_MEMBER2 = 2      /* second level: the object holds a pointer at byte offset1, and the key
+    RSBD8G_MEMBER2 = 2,     /* second level: the object holds a pointer at byte offset1, and the key
                                sits at byte offset2 behind that pointer */
+    RSBD8G_KEYED = 3        /* rsbd8g_radixsortcopy_keyed only: the keys come in a separate array */
 };
 
 /* diagnostics only: tile 1 of every scatter pass never publishes its look-back state, so
@@ -105,6 +106,15 @@ RSBD8G_API rsbd8g_status rsbd8g_scratch_bytes(const rsbd8g_desc *desc, size_t co
  * member pointer :61242; type+offset :61359-61739). */
 RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy(const rsbd8g_desc *desc, size_t count,
                                               const void *input, void *output, rsbd8g_stream stream);
+
+/* Sort the `count` 8-byte values of `input` (object pointers) into `output` by the keys in
+ * `keys` (count raw keys of desc->key_bytes each, same index), with desc->indirection ==
+ * RSBD8G_KEYED.  Allocates, blocks until done.  The C++ facade uses it for getter
+ * indirection, whose keys it evaluates on the host.
+ * Replaces: rsbd8::radixsortcopy<&V::getter, ...> (Radixsortbidi8.hpp:61242 with a member
+ * function pointer; the getter call itself is splitget, Radixsortbidi8.hpp:2405-2719). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                    const void *input, void *output, rsbd8g_stream stream);
 
 /* Sort `count` elements of `input` in place.  Allocates, blocks until done.
  * Replaces: rsbd8::radixsort (Radixsortbidi8.hpp:60398). */

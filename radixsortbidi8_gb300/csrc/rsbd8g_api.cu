@@ -17,7 +17,7 @@
 
 #include "rsbd8g.h"
 #include "rsbd8g_internal.h"
-#include "rsbd8g_kernels.cuh"
+#include "rsbd8g_device.cuh"
 
 namespace rsbd8g {
 
@@ -28,11 +28,7 @@ constexpr size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 constexpr uint64_t kMaxCount = uint64_t(1) << 40;
 constexpr uint64_t kNarrowStatusLimit = uint64_t(1) << 30;  // 30-bit look-back counts below this
 
-// tile geometry of the onesweep pass (keys per tile = THREADS * ITEMS)
-constexpr int kSweepThreads = 512;
-constexpr int kSweepItemsDirect = 16;
-constexpr int kSweepItemsIndirect = 8;
-constexpr int kHistThreads = 512;
+}  // namespace
 
 int device_sms(int dev) {
     static int cache[64] = {0};
@@ -44,8 +40,6 @@ int device_sms(int dev) {
     }
     return cache[dev];
 }
-
-}  // namespace
 
 // ---- launch profiling -----------------------------------------------------------------------
 
@@ -77,44 +71,41 @@ cudaEvent_t prof_event() {
 }
 }  // namespace
 
-// run `launch` (which enqueues one kernel on s), bracketed by events while profiling is on
-template <class F>
-cudaError_t timed_launch(cudaStream_t s, uint32_t kernel, uint32_t key_bytes, uint32_t pass, uint64_t n, F &&launch) {
+LaunchTimer::LaunchTimer(cudaStream_t s, uint32_t kernel, uint32_t key_bytes, uint32_t pass, uint64_t n)
+    : s_(s), a_(nullptr), b_(nullptr) {
     ProfState &p = prof();
     bool on;
     {
         std::lock_guard<std::mutex> g(p.mu);
         on = p.on;
     }
-    if (on) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(s, &cs);
-        if (cs != cudaStreamCaptureStatusNone) on = false;
-    }
-    if (!on) {
-        launch();
-        return cudaGetLastError();
-    }
-    cudaEvent_t a, b;
+    if (!on) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return;
     {
         std::lock_guard<std::mutex> g(p.mu);
-        a = prof_event();
-        b = prof_event();
+        a_ = prof_event();
+        b_ = prof_event();
     }
-    cudaEventRecord(a, s);
-    launch();
-    cudaError_t e = cudaGetLastError();
-    cudaEventRecord(b, s);
+    rec_ = rsbd8g_launch_record{};
+    rec_.kernel = kernel;
+    rec_.key_bytes = key_bytes;
+    rec_.pass = pass;
+    rec_.count = n;
+    cudaEventRecord(a_, s);
+}
+
+LaunchTimer::~LaunchTimer() {
+    if (!a_) return;
+    cudaEventRecord(b_, s_);
+    ProfState &p = prof();
     std::lock_guard<std::mutex> g(p.mu);
     ProfRec pr{};
-    pr.r.kernel = kernel;
-    pr.r.key_bytes = key_bytes;
-    pr.r.pass = pass;
-    pr.r.count = n;
-    pr.a = a;
-    pr.b = b;
+    pr.r = rec_;
+    pr.a = a_;
+    pr.b = b_;
     p.recs.push_back(pr);
-    return e;
 }
 
 rsbd8g_status profile_enable(int enable) {
@@ -150,7 +141,7 @@ rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
     const uint32_t mode = d->mode, dir = d->direction;
     if (!(mode < 8u || (mode >= 64u && mode <= 66u))) return RSBD8G_ERR_BAD_ARG;
     if (dir > 3u) return RSBD8G_ERR_BAD_ARG;
-    if (d->indirection > RSBD8G_MEMBER2) return RSBD8G_ERR_BAD_ARG;
+    if (d->indirection > RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
     const bool is_signed = d->key_kind == RSBD8G_KIND_SIGNED || d->key_kind == RSBD8G_KIND_FLOAT;
     const bool is_float = d->key_kind == RSBD8G_KIND_FLOAT;
     Filter f;
@@ -167,12 +158,14 @@ rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
     r->off1 = d->offset1;
     r->off2 = d->offset2;
     r->flags = d->flags;
+    r->keys = nullptr;
     return RSBD8G_OK;
 }
 
 Layout layout_for(const Resolved &r, uint64_t n) {
     Layout L{};
-    const int tile = kSweepThreads * (r.indirect ? kSweepItemsIndirect : kSweepItemsDirect);
+    const SweepGeometry g = sweep_geometry(int(r.key_bytes), r.indirect != 0);
+    const int tile = g.threads * g.items;
     L.num_tiles = uint32_t((n + tile - 1) / tile);
     L.wide_status = n >= kNarrowStatusLimit;
     const size_t sw = L.wide_status ? 8 : 4;
@@ -190,103 +183,6 @@ Layout layout_for(const Resolved &r, uint64_t n) {
     return L;
 }
 
-namespace {
-
-template <typename U, bool HAS_VAL, typename S>
-cudaError_t launch_sweeps(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, cudaStream_t s) {
-    constexpr int ITEMS = HAS_VAL ? kSweepItemsIndirect : kSweepItemsDirect;
-    using SM = OnesweepSmem<U, HAS_VAL, kSweepThreads, ITEMS>;
-    auto kern = k_onesweep<U, HAS_VAL, kSweepThreads, ITEMS, S>;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    static std::once_flag once[64];
-    static int occ[64];
-    std::call_once(once[dev & 63], [&] {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SM::kBytes));
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kSweepThreads, SM::kBytes);
-        occ[dev & 63] = b > 0 ? b : 1;
-    });
-    const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, uint64_t(occ[dev & 63]) * device_sms(dev)));
-    Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
-    const unsigned long long *bstart = reinterpret_cast<const unsigned long long *>(scratch + L.bstart);
-    const Filter f = r.f;
-    for (uint32_t p = 0; p < r.key_bytes; ++p) {
-        S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
-        cudaError_t e = timed_launch(s, RSBD8G_KERNEL_ONESWEEP, r.key_bytes, p, n, [&] {
-            kern<<<grid, kSweepThreads, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, f);
-        });
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-
-template <typename U>
-cudaError_t launch_histogram(const Resolved &r, uint64_t n, const void *in, const Layout &L, unsigned char *scratch,
-                             cudaStream_t s) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const uint64_t per_cta = uint64_t(kHistThreads) * 64;   // keys per CTA sweep, to size the grid
-    const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per_cta - 1) / per_cta,
-                                                                            uint64_t(device_sms(dev)) * 4)));
-    unsigned long long *ghist = reinterpret_cast<unsigned long long *>(scratch + L.ghist);
-    return timed_launch(s, RSBD8G_KERNEL_HISTOGRAM, r.key_bytes, 0, n, [&] {
-        if (r.indirect) {
-            k_gather_histogram<U, kHistThreads><<<grid, kHistThreads, 0, s>>>(
-                static_cast<const uint64_t *>(in), n, r.f, r.off1, r.off2, int(r.indirect),
-                reinterpret_cast<U *>(scratch + L.keys_a), ghist);
-        } else {
-            k_histogram<U, kHistThreads><<<grid, kHistThreads, 0, s>>>(static_cast<const U *>(in), n, r.f, ghist);
-        }
-    });
-}
-
-template <typename U>
-cudaError_t launch_all(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in,
-                       void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
-    cudaError_t e = timed_launch(s, RSBD8G_KERNEL_MEMSET, r.key_bytes, 0, n,
-                                 [&] { cudaMemsetAsync(scratch, 0, L.zero_bytes, s); });
-    if (e != cudaSuccess) return e;
-    if ((e = launch_histogram<U>(r, n, in, L, scratch, s)) != cudaSuccess) return e;
-    PlanArgs a{};
-    a.in = in;
-    a.out = out;
-    a.buf = buf;
-    a.keys_a = r.indirect ? scratch + L.keys_a : nullptr;
-    a.keys_b = r.indirect ? scratch + L.keys_b : nullptr;
-    a.elem_bytes = r.elem_bytes;
-    a.inplace = inplace;
-    a.to_buffer = to_buffer;
-    a.rev = r.rev;
-    a.indirect = r.indirect != 0;
-    a.passes = r.key_bytes;
-    const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
-    a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
-    a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;
-    e = timed_launch(s, RSBD8G_KERNEL_PLAN, r.key_bytes, 0, n, [&] {
-        k_plan<<<1, 256, 0, s>>>(reinterpret_cast<Control *>(scratch + L.ctrl),
-                                 reinterpret_cast<const unsigned long long *>(scratch + L.ghist),
-                                 reinterpret_cast<unsigned long long *>(scratch + L.bstart), n, a);
-    });
-    if (e != cudaSuccess) return e;
-    if (r.indirect) {
-        e = L.wide_status ? launch_sweeps<U, true, uint64_t>(r, n, L, scratch, s)
-                          : launch_sweeps<U, true, uint32_t>(r, n, L, scratch, s);
-    } else {
-        e = L.wide_status ? launch_sweeps<U, false, uint64_t>(r, n, L, scratch, s)
-                          : launch_sweeps<U, false, uint32_t>(r, n, L, scratch, s);
-    }
-    if (e != cudaSuccess) return e;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const uint32_t cgrid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(device_sms(dev)) * 8)));
-    return timed_launch(s, RSBD8G_KERNEL_COPY, r.key_bytes, 0, n, [&] {
-        k_copy<<<cgrid, 256, 0, s>>>(reinterpret_cast<const Control *>(scratch + L.ctrl), n);
-    });
-}
-
-}  // namespace
-
 rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
                            void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
     if (n > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
@@ -296,10 +192,10 @@ rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t 
     unsigned char *sc = static_cast<unsigned char *>(scratch);
     cudaError_t e;
     switch (r.key_bytes) {
-        case 1: e = launch_all<uint8_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
-        case 2: e = launch_all<uint16_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
-        case 4: e = launch_all<uint32_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
-        default: e = launch_all<uint64_t>(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 1: e = launch_sort_k1(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 2: e = launch_sort_k2(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 4: e = launch_sort_k4(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        default: e = launch_sort_k8(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
     }
     return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
 }
@@ -366,6 +262,7 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortcopynoalloc(const rsbd8g_desc *desc, si
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
+    if (r.indirect == RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
     if (count == 0) return RSBD8G_OK;
     if (!input || !output) return RSBD8G_ERR_BAD_ARG;
     if (input == output) return RSBD8G_ERR_BAD_ARG;
@@ -384,6 +281,7 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
+    if (r.indirect == RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
     if (count == 0) return RSBD8G_OK;
     if (!input) return RSBD8G_ERR_BAD_ARG;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -404,10 +302,11 @@ RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stre
 // allocating forms: one stream-ordered allocation of buffer + scratch, freed on the stream;
 // the call waits for the sort, as the reference's functions return only when sorted
 static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const void *input, void *output, bool inplace,
-                                rsbd8g_stream stream) {
+                                rsbd8g_stream stream, const void *keys) {
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
+    r.keys = keys;
     if (count > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (count <= 1) {
@@ -439,11 +338,20 @@ static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const voi
 
 RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy(const rsbd8g_desc *desc, size_t count, const void *input, void *output,
                                               rsbd8g_stream stream) {
-    return sort_alloc(desc, count, input, output, false, stream);
+    if (desc && desc->indirection == RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
+    return sort_alloc(desc, count, input, output, false, stream, nullptr);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                    const void *input, void *output, rsbd8g_stream stream) {
+    if (!desc || desc->indirection != RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
+    if (count > 1 && !keys) return RSBD8G_ERR_BAD_ARG;
+    return sort_alloc(desc, count, input, output, false, stream, keys);
 }
 
 RSBD8G_API rsbd8g_status rsbd8g_radixsort(const rsbd8g_desc *desc, size_t count, void *input, rsbd8g_stream stream) {
-    return sort_alloc(desc, count, input, nullptr, true, stream);
+    if (desc && desc->indirection == RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
+    return sort_alloc(desc, count, input, nullptr, true, stream, nullptr);
 }
 
 }  // extern "C"

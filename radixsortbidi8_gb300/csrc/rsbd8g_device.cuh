@@ -15,6 +15,7 @@
 // identical.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace rsbd8g {
@@ -64,24 +65,33 @@ static_assert(sizeof(Control) <= 1024, "control block must fit its slot");
 
 // ---- key filter -----------------------------------------------------------------------
 
-// K(b): transform raw key bits into an unsigned key whose ascending order is the
-// reference's order for the resolved mode; descending sorts use the complement.
-template <typename U>
-__device__ __forceinline__ U sortkey(U b, const Filter &f) {
+// K(b): transform raw key bits into an unsigned key whose ascending order is the reference's
+// ascending order for the filter combination MODE = isabsvalue | issignmode << 1 | isfltpmode << 2
+// (the low three bits of the resolved sortingmode).  Descending sorts use the complement ~K,
+// which the kernels apply per digit.
+template <int MODE, typename U>
+__device__ __forceinline__ U filter_key(U b) {
+    constexpr bool ABS = (MODE & 1) != 0, SIGN = (MODE & 2) != 0, FLTP = (MODE & 4) != 0;
     constexpr int W = int(sizeof(U)) * 8;
-    const U sb = U(U(1) << (W - 1));
-    const U s = (b & sb) ? U(~U(0)) : U(0);   // sign mask
-    const U m = U(b & U(~sb));
-    U k;
-    if (f.absv != f.fltp) {
-        if (f.absv) k = f.sign ? U(U(b + s) ^ s) : U(U(b << 1) ^ s);      // abs signed / tiered abs signed
-        else k = f.sign ? U(U(U(m + s) ^ s) ^ sb) : U(m ^ s);              // float (+MSB flip) / inside-out float
-    } else if (f.absv) {
-        k = f.sign ? m : U(U(U(b << 1) | U(b >> (W - 1))) ^ U(1));        // abs float / tiered abs float
+    constexpr U sb = U(U(1) << (W - 1));
+    using I = typename std::make_signed<U>::type;
+    if constexpr (ABS != FLTP) {
+        const U s = U(I(b) >> (W - 1));            // sign mask: all ones for negative keys
+        if constexpr (ABS) {
+            if constexpr (SIGN) return U(U(b + s) ^ s);                      // absolute signed
+            else return U(U(b << 1) ^ s);                                    // tiered absolute signed
+        } else {
+            const U m = U(b & U(~sb));
+            if constexpr (SIGN) return U(U(U(m + s) ^ s) ^ sb);              // floating point, MSB flip
+            else return U(m ^ s);                                            // inside-out floating point
+        }
+    } else if constexpr (ABS) {
+        if constexpr (SIGN) return U(b & U(~sb));                           // absolute floating point
+        else return U(U(U(b << 1) | U(b >> (W - 1))) ^ U(1));                // tiered abs float: rotl 1, LSB flip
     } else {
-        k = f.sign ? U(b ^ sb) : b;                                         // signed (MSB flip) / unsigned
+        if constexpr (SIGN) return U(b ^ sb);                                // signed, MSB flip
+        else return b;                                                       // unsigned
     }
-    return f.desc ? U(~k) : k;
 }
 
 template <typename U>

@@ -19,6 +19,7 @@ struct Resolved {
     uint32_t indirect;    // RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2
     uint32_t flags;
     int64_t off1, off2;
+    const void *keys;     // RSBD8G_KEYED: the caller's key array
 };
 
 // byte offsets of the parts of a scratch area
@@ -27,6 +28,39 @@ struct Layout {
     uint32_t num_tiles;
     bool wide_status;
 };
+
+// brackets one kernel launch with CUDA events on its stream while launch profiling is on
+class LaunchTimer {
+public:
+    LaunchTimer(cudaStream_t s, uint32_t kernel, uint32_t key_bytes, uint32_t pass, uint64_t n);
+    ~LaunchTimer();
+    LaunchTimer(const LaunchTimer &) = delete;
+    LaunchTimer &operator=(const LaunchTimer &) = delete;
+
+private:
+    cudaStream_t s_;
+    cudaEvent_t a_, b_;
+    rsbd8g_launch_record rec_{};
+};
+
+int device_sms(int dev);
+
+// the launch sequence of one sort, per key size (rsbd8g_sort_k{1,2,4,8}.cu)
+#define RSBD8G_DECLARE_LAUNCH(name)                                                                          \
+    cudaError_t name(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in, \
+                     void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);
+RSBD8G_DECLARE_LAUNCH(launch_sort_k1)
+RSBD8G_DECLARE_LAUNCH(launch_sort_k2)
+RSBD8G_DECLARE_LAUNCH(launch_sort_k4)
+RSBD8G_DECLARE_LAUNCH(launch_sort_k8)
+
+// tile geometry of the onesweep passes, per key size (keys per tile = threads * items)
+struct SweepGeometry {
+    int threads, items;
+};
+constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
+    return indirect ? SweepGeometry{256, 8} : SweepGeometry{256, key_bytes == 8 ? 12 : 16};
+}
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
 Layout layout_for(const Resolved &r, uint64_t n);

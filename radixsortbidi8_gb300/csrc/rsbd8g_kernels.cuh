@@ -1,9 +1,9 @@
 // rsbd8g_kernels.cuh - the sm_103a kernels of the stable LSD radix sort.
 //
 //   k_histogram / k_gather_histogram   all 256-bin digit histograms in one read of the keys,
-//                                      with warp-aggregated (__match_any_sync) shared-memory
-//                                      atomics; the gather form reads the key through each
-//                                      object pointer and writes the filtered keys once
+//                                      with warp-aggregated shared-memory atomics over several
+//                                      sub-histogram copies; the gather form reads the key through
+//                                      each object pointer and writes the filtered keys once
 //   k_plan                             exclusive scan of every digit histogram, the reference's
 //                                      pass-skip test, and the ping-pong plan of the passes
 //   k_onesweep                         one stable scatter pass of a surviving digit: persistent
@@ -21,34 +21,53 @@ namespace rsbd8g {
 
 // ---- up-front histograms --------------------------------------------------------------------
 
-// add 1 to h[d] for every lane, aggregated over the lanes of the warp that share d
-__device__ __forceinline__ void warp_agg_add(uint32_t *h, uint32_t d, bool valid, uint32_t lane) {
-    const uint32_t key = valid ? d : 0xFFFFFFFFu;
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-    if (valid && lane == uint32_t(__ffs(peers) - 1)) atomicAdd(h + d, uint32_t(__popc(peers)));
+// Histogram counting: each CTA keeps kHistCopies sub-histograms (P digits x 256 bins, u32) in
+// shared memory and its warps spread over them, so warps rarely collide on a bin.  A warp whose
+// lanes all share the digit (a skewed digit, e.g. the zero top bytes of small keys) adds 32 with
+// one atomic instead of 32 conflicting ones.
+constexpr int kHistCopies = 4;
+
+__device__ __forceinline__ void hist_add(uint32_t *h, uint32_t d, bool valid) {
+    const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+    const bool v0 = __shfl_sync(0xFFFFFFFFu, valid, 0);
+    if (__all_sync(0xFFFFFFFFu, valid && d == d0)) {
+        if ((threadIdx.x & 31u) == 0 && v0) atomicAdd(h + d0, 32u);
+    } else if (valid) {
+        atomicAdd(h + d, 1u);
+    }
 }
 
 template <typename U>
-__device__ __forceinline__ void count_key(uint32_t *sh, U k, bool valid, uint32_t lane) {
+__device__ __forceinline__ void count_key(uint32_t *sh, U k, bool valid, uint32_t dmask) {
 #pragma unroll
-    for (int p = 0; p < int(sizeof(U)); ++p) warp_agg_add(sh + p * kBuckets, digit_of(k, p), valid, lane);
+    for (int p = 0; p < int(sizeof(U)); ++p) hist_add(sh + p * kBuckets, digit_of(k, p) ^ dmask, valid);
+}
+
+template <int THREADS, int P>
+__device__ __forceinline__ void zero_hist(uint32_t *sh) {
+    for (int i = threadIdx.x; i < kHistCopies * P * kBuckets; i += THREADS) sh[i] = 0;
+    __syncthreads();
 }
 
 template <int THREADS, int P>
 __device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long long *ghist) {
     __syncthreads();
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS)
-        if (sh[i]) atomicAdd(ghist + i, (unsigned long long)sh[i]);
+    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int c = 0; c < kHistCopies; ++c) v += sh[c * P * kBuckets + i];
+        if (v) atomicAdd(ghist + i, (unsigned long long)v);
+    }
 }
 
-template <typename U, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, Filter f,
+template <typename U, int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, uint32_t dmask,
                                                        unsigned long long *__restrict__ ghist) {
     constexpr int P = int(sizeof(U));
     constexpr int V = 16 / int(sizeof(U));
-    __shared__ uint32_t sh[P * kBuckets];
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) sh[i] = 0;
-    __syncthreads();
+    __shared__ uint32_t shall[kHistCopies * P * kBuckets];
+    zero_hist<THREADS, P>(shall);
+    uint32_t *sh = shall + ((threadIdx.x >> 5) % kHistCopies) * P * kBuckets;
     const uint32_t lane = threadIdx.x & 31u;
     // scalar head up to 16-byte alignment, vector body, scalar tail
     const uint64_t mis = (reinterpret_cast<uintptr_t>(keys) & 15u) / sizeof(U);
@@ -61,12 +80,12 @@ __global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ key
         for (uint64_t b = 0; b < head; b += 32) {
             const uint64_t i = b + lane;
             const bool ok = i < head;
-            count_key(sh, sortkey(ok ? keys[i] : U(0), f), ok, lane);
+            count_key(sh, filter_key<MODE>(ok ? keys[i] : U(0)), ok, dmask);
         }
         for (uint64_t b = tail0; b < n; b += 32) {
             const uint64_t i = b + lane;
             const bool ok = i < n;
-            count_key(sh, sortkey(ok ? keys[i] : U(0), f), ok, lane);
+            count_key(sh, filter_key<MODE>(ok ? keys[i] : U(0)), ok, dmask);
         }
     }
     const uint4 *kv = reinterpret_cast<const uint4 *>(keys + head);
@@ -84,22 +103,24 @@ __global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ key
             U k[V];
             memcpy(k, &v[u], 16);
 #pragma unroll
-            for (int j = 0; j < V; ++j) count_key(sh, sortkey(k[j], f), ok, lane);
+            for (int j = 0; j < V; ++j) count_key(sh, filter_key<MODE>(k[j]), ok, dmask);
         }
     }
-    flush_hist<THREADS, P>(sh, ghist);
+    flush_hist<THREADS, P>(shall, ghist);
 }
 
-// indirect form: gather the key through each object pointer, write the filtered key
-template <typename U, int THREADS>
+// indirect form: gather the key through each object pointer (level 1: at off1; level 2: behind the
+// pointer held at off1, at off2; level 3: keys_in[i], supplied by the caller), write the filtered key
+template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__restrict__ ptrs, uint64_t n,
-                                                              Filter f, int64_t off1, int64_t off2, int level,
+                                                              uint32_t dmask, int64_t off1, int64_t off2, int level,
+                                                              const U *__restrict__ keys_in,
                                                               U *__restrict__ keys_out,
                                                               unsigned long long *__restrict__ ghist) {
     constexpr int P = int(sizeof(U));
-    __shared__ uint32_t sh[P * kBuckets];
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) sh[i] = 0;
-    __syncthreads();
+    __shared__ uint32_t shall[kHistCopies * P * kBuckets];
+    zero_hist<THREADS, P>(shall);
+    uint32_t *sh = shall + ((threadIdx.x >> 5) % kHistCopies) * P * kBuckets;
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t gwarp = (uint64_t(blockIdx.x) * THREADS + threadIdx.x) >> 5;
     const uint64_t nwarps = (uint64_t(gridDim.x) * THREADS) >> 5;
@@ -111,21 +132,26 @@ __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__
             const uint64_t i = b + u * 32 + lane;
             raw[u] = 0;
             if (i < n) {
-                const unsigned char *obj = reinterpret_cast<const unsigned char *>(ptrs[i]) + off1;
-                if (level == 2) obj = load_ptr(obj) + off2;
-                raw[u] = load_member<U>(obj);
+                if (level == 3) {
+                    raw[u] = keys_in[i];
+                } else {
+                    const unsigned char *obj = reinterpret_cast<const unsigned char *>(ptrs[i]) + off1;
+                    if (level == 2) obj = load_ptr(obj) + off2;
+                    raw[u] = load_member<U>(obj);
+                }
             }
         }
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const uint64_t i = b + u * 32 + lane;
             const bool ok = i < n;
-            const U k = sortkey(raw[u], f);
+            // the stored key is final: filtered, and complemented for descending sorts
+            const U k = dmask ? U(~filter_key<MODE>(raw[u])) : filter_key<MODE>(raw[u]);
             if (ok) keys_out[i] = k;
-            count_key(sh, k, ok, lane);
+            count_key(sh, k, ok, 0u);
         }
     }
-    flush_hist<THREADS, P>(sh, ghist);
+    flush_hist<THREADS, P>(shall, ghist);
 }
 
 // ---- scan, pass-skip and plan -----------------------------------------------------------------
@@ -147,7 +173,7 @@ struct PlanArgs {
 };
 
 // one CTA of 256 threads
-__global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
+static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
                                               unsigned long long *__restrict__ bstart, uint64_t n, PlanArgs a) {
     __shared__ unsigned long long wsum[8];
     __shared__ int skip[kMaxPasses];
@@ -227,38 +253,63 @@ __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl, const 
 
 // ---- the onesweep scatter pass ----------------------------------------------------------------
 
+// Tile geometry: THREADS threads (a multiple of 256 is not required, but at least 256: thread d
+// owns digit d in the per-digit phases), ITEMS keys per thread, TILE = THREADS * ITEMS keys.
 template <typename U, bool HAS_VAL, int THREADS, int ITEMS>
 struct OnesweepSmem {
     static constexpr int kTile = THREADS * ITEMS;
     static constexpr int kWarps = THREADS / 32;
-    static constexpr int kHistStride = kBuckets + 1;  // + one slot for out-of-range items
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
     static constexpr size_t kStageV = HAS_VAL ? size_t(kTile) * 8 : 0;
     static constexpr size_t kOffV = (kStageK + 15) & ~size_t(15);
-    static constexpr size_t kOffHist = kOffV + kStageV;
-    static constexpr size_t kOffTileStart = kOffHist + size_t(kWarps) * kHistStride * 4;
-    static constexpr size_t kOffGofs = (kOffTileStart + kBuckets * 4 + 15) & ~size_t(15);
-    static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;
-    static constexpr size_t kOffMisc = kOffBstart + kBuckets * 8;
+    static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32 [WARPS][256]
+    static constexpr size_t kOffGofs = kOffWofs + size_t(kWarps) * kBuckets * 4;  // i64 [256]
+    static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;              // u64 [256]
+    static constexpr size_t kOffMisc = kOffBstart + kBuckets * 8;              // u32 [16]
     static constexpr size_t kBytes = kOffMisc + 64;
 };
 
-template <typename U, bool HAS_VAL, int THREADS, int ITEMS, typename S>
-__global__ void __launch_bounds__(THREADS, (sizeof(U) <= 4 && !HAS_VAL) ? 2 : 1)
+// the digit of key k for this pass: filtered key (compile-time mode), byte `pass`, complemented
+// for descending sorts (dmask = 0xFF) -- the descending order is the ascending order of ~K
+template <int MODE, typename U>
+__device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
+    return (uint32_t(filter_key<MODE>(k) >> (pass * kRadixBits)) & (kBuckets - 1)) ^ dmask;
+}
+
+// peer mask of the lanes holding the same 8-bit digit (ballot per bit)
+__device__ __forceinline__ uint32_t match_digit(uint32_t d) {
+    uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < kRadixBits; ++k) {
+        const bool bit = (d >> k) & 1u;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, bit);
+        peers &= bit ? b : ~b;
+    }
+    return peers;
+}
+
+// resident CTAs per SM the register allocation is bounded for
+template <typename U, bool HAS_VAL>
+constexpr int onesweep_min_blocks() {
+    return HAS_VAL ? 3 : (sizeof(U) <= 4 ? 4 : 3);
+}
+
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
     k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
-               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, Filter f) {
+               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     constexpr int TILE = L::kTile;
     constexpr int WARPS = L::kWarps;
-    constexpr int HS = L::kHistStride;
+    static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
+    static_assert(TILE <= 65535, "tile ranks are 16-bit");
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage_k = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
-    uint32_t *whist = reinterpret_cast<uint32_t *>(smem + L::kOffHist);
-    uint32_t *tile_start = reinterpret_cast<uint32_t *>(smem + L::kOffTileStart);
+    uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
-    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [0] tile, [1] bad, [2..9] scan
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [0] tile [1] bad [2..9] scan
 
     const PassPlan plan = ctrl->plan[pass];
     if (!plan.active) return;
@@ -269,78 +320,87 @@ __global__ void __launch_bounds__(THREADS, (sizeof(U) <= 4 && !HAS_VAL) ? 2 : 1)
     const bool reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
-    S *__restrict__ st_pass = status;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
-    const Filter fk = HAS_VAL ? Filter{0, 0, 0, 0} : f;   // indirect passes carry filtered keys
+    uint32_t *wcnt = wofs + warp * kBuckets;   // this warp's digit counters, later its offsets
+    const uint32_t ltmask = lanemask_lt();
 
     for (;;) {
         if (tid == 0) {
             misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
             misc[1] = 0;
         }
+        for (int i = lane; i < kBuckets; i += 32) wcnt[i] = 0;
         __syncthreads();
         const uint32_t tile = misc[0];
         if (tile >= num_tiles) break;
         const uint64_t tbase = uint64_t(tile) * TILE;
         const uint32_t tvalid = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
 
-        // zero this warp's digit counters
-        uint32_t *wh = whist + warp * HS;
-        for (int i = lane; i < HS; i += 32) wh[i] = 0;
-        __syncwarp();
-
-        // load ITEMS keys per thread, warp-striped (item i of lane l = tile slot w*32*ITEMS + i*32 + l)
+        // load ITEMS keys per thread, warp-striped: item i of lane l is slot w*32*ITEMS + i*32 + l.
+        // Slots past the end get digit 255: they rank after every real key of the tile.
         U keys[ITEMS];
         uint64_t vals[HAS_VAL ? ITEMS : 1];
-        uint32_t dig[ITEMS];
+        uint32_t dr[ITEMS];      // digit, later (rank << 8) | digit
+        const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
+        if (!reverse && tvalid == TILE) {
+            const U *p = src_k + tbase + slot0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t slot = uint32_t(warp) * 32u * ITEMS + uint32_t(i) * 32u + uint32_t(lane);
-            const bool ok = slot < tvalid;
-            const uint64_t gi = tbase + slot;
-            const uint64_t si = reverse ? (n - 1u - gi) : gi;
-            keys[i] = ok ? src_k[si] : U(0);
-            if constexpr (HAS_VAL) vals[i] = ok ? src_v[si] : 0ull;
-            dig[i] = ok ? digit_of(sortkey(keys[i], fk), pass) : uint32_t(kBuckets);
-        }
-        // warp multisplit rank: stable in slot order
-        uint32_t rank[ITEMS];
-        const uint32_t ltmask = lanemask_lt();
+            for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+            if constexpr (HAS_VAL) {
+                const uint64_t *q = src_v + tbase + slot0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dig[i]);
-            const int leader = __ffs(peers) - 1;
-            uint32_t base = 0;
-            if (lane == leader) {
-                base = wh[dig[i]];
-                wh[dig[i]] = base + uint32_t(__popc(peers));
+                for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 32];
             }
-            base = __shfl_sync(0xFFFFFFFFu, base, leader);
-            rank[i] = base + uint32_t(__popc(peers & ltmask));
+        } else {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                const uint64_t gi = tbase + slot;
+                const uint64_t si = reverse ? (n - 1u - gi) : gi;
+                const bool ok = slot < tvalid;
+                keys[i] = ok ? src_k[si] : U(~U(0));
+                if constexpr (HAS_VAL) vals[i] = ok ? src_v[si] : 0ull;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t slot = slot0 + uint32_t(i) * 32u;
+            dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
+        }
+        // warp multisplit: peer masks first (independent), then the counter chain in slot order
+        uint32_t peers[ITEMS];
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) peers[i] = match_digit(dr[i]);
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = dr[i];
+            const uint32_t before = wcnt[d];
             __syncwarp();
+            const uint32_t lower = uint32_t(__popc(peers[i] & ltmask));
+            if (lower == 0) wcnt[d] = before + uint32_t(__popc(peers[i]));
+            __syncwarp();
+            dr[i] = ((before + lower) << 8) | d;
         }
         __syncthreads();
 
-        // per digit: exclusive offsets of the warps, tile count; publish the tile aggregate
-        uint32_t count = 0;
+        // per digit: exclusive offsets of the warps and the tile count; publish the aggregate
+        uint32_t count = 0, x = 0;
         if (tid < kBuckets) {
             uint32_t run = 0;
-#pragma unroll 4
+#pragma unroll
             for (int w2 = 0; w2 < WARPS; ++w2) {
-                const uint32_t c = whist[w2 * HS + tid];
-                whist[w2 * HS + tid] = run;
+                const uint32_t c = wofs[w2 * kBuckets + tid];
+                wofs[w2 * kBuckets + tid] = run;
                 run += c;
             }
             count = run;
+            if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalid;   // the padding slots
             if (tile != stall_tile)
-                st_relaxed(st_pass + size_t(tile) * kBuckets + tid,
+                st_relaxed(status + size_t(tile) * kBuckets + tid,
                            StatusWord<S>::make(tile == 0 ? kStInclusive : kStAggregate, count));
-        }
-        // exclusive scan of the tile counts over the digits
-        uint32_t x = count;
-        if (tid < kBuckets) {
+            x = run;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
@@ -352,39 +412,53 @@ __global__ void __launch_bounds__(THREADS, (sizeof(U) <= 4 && !HAS_VAL) ? 2 : 1)
         if (tid < kBuckets) {
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
-            const uint32_t ts = before + x - count;
-            tile_start[tid] = ts;
-            // decoupled look-back over the predecessors' states for digit tid (bounded wait)
+            const uint32_t ts = before + x - (count + (tid == kBuckets - 1 ? uint32_t(TILE) - tvalid : 0u));
+#pragma unroll
+            for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * kBuckets + tid] += ts;
+            // decoupled look-back for digit tid: read predecessors four at a time (bounded wait)
             uint64_t excl = 0;
             bool bad = false;
             if (tile > 0) {
                 int64_t j = int64_t(tile) - 1;
                 uint32_t spins = 0;
                 uint64_t t0 = 0;
-                while (j >= 0) {
-                    const S wv = ld_relaxed(st_pass + size_t(j) * kBuckets + tid);
-                    const uint32_t s = StatusWord<S>::state(wv);
-                    if (s == kStInvalid) {
-                        if (++spins > 32u) {
-                            if (*reinterpret_cast<volatile uint32_t *>(&ctrl->abort)) { bad = true; break; }
-                            const uint64_t now = globaltimer_ns();
-                            if (t0 == 0) t0 = now;
-                            else if (now - t0 > spin_limit) {
-                                atomicOr(&ctrl->error, kDevTimeout);
-                                atomicExch(&ctrl->abort, 1u);
-                                bad = true;
-                                break;
-                            }
-                            __nanosleep(64);
+                bool done = false;
+                while (!done && j >= 0) {
+                    S w4[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        w4[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + tid) : S(0);
+                    int q = 0;
+                    for (; q < 4 && j - q >= 0; ++q) {
+                        const uint32_t st = StatusWord<S>::state(w4[q]);
+                        if (st == kStInvalid) break;
+                        excl += StatusWord<S>::value(w4[q]);
+                        if (st == kStInclusive) {
+                            done = true;
+                            break;
                         }
+                    }
+                    if (done) break;
+                    if (q == 4) {          // four aggregates: keep walking back
+                        j -= 4;
                         continue;
                     }
-                    excl += StatusWord<S>::value(wv);
-                    if (s == kStInclusive) break;
-                    --j;
+                    j -= q;                // wait on the first unpublished predecessor
+                    if (++spins > 16u) {
+                        if (*reinterpret_cast<volatile uint32_t *>(&ctrl->abort)) { bad = true; break; }
+                        const uint64_t now = globaltimer_ns();
+                        if (t0 == 0) t0 = now;
+                        else if (now - t0 > spin_limit) {
+                            atomicOr(&ctrl->error, kDevTimeout);
+                            atomicExch(&ctrl->abort, 1u);
+                            bad = true;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
                 }
                 if (tile != stall_tile)
-                    st_relaxed(st_pass + size_t(tile) * kBuckets + tid,
+                    st_relaxed(status + size_t(tile) * kBuckets + tid,
                                StatusWord<S>::make(kStInclusive, excl + count));
             }
             if (bad) misc[1] = 1u;
@@ -393,25 +467,35 @@ __global__ void __launch_bounds__(THREADS, (sizeof(U) <= 4 && !HAS_VAL) ? 2 : 1)
         __syncthreads();
         const bool tile_bad = misc[1] != 0 || tile == stall_tile;
 
-        // stage the tile in shared memory, sorted by digit
+        // stage the tile in shared memory, sorted by digit (padding slots land past tvalid)
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            if (dig[i] < uint32_t(kBuckets)) {
-                const uint32_t pos = tile_start[dig[i]] + wh[dig[i]] + rank[i];
-                stage_k[pos] = keys[i];
-                if constexpr (HAS_VAL) stage_v[pos] = vals[i];
-            }
+            const uint32_t pos = wcnt[dr[i] & 0xFFu] + (dr[i] >> 8);
+            stage_k[pos] = keys[i];
+            if constexpr (HAS_VAL) stage_v[pos] = vals[i];
         }
         __syncthreads();
         // write out: consecutive threads take consecutive slots of a bucket run
         if (!tile_bad) {
-            for (uint32_t s = tid; s < tvalid; s += THREADS) {
-                const U k = stage_k[s];
-                const uint32_t d = digit_of(sortkey(k, fk), pass);
-                const long long g = gofs[d] + (long long)s;
-                if (g >= 0 && uint64_t(g) < n) {
-                    if (dst_k) dst_k[g] = k;
-                    if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+            if (tvalid == TILE) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) {
+                    const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
+                    const U k = stage_k[s];
+                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    if (uint64_t(g) < n) {
+                        if (dst_k) dst_k[g] = k;
+                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    }
+                }
+            } else {
+                for (uint32_t s = tid; s < tvalid; s += THREADS) {
+                    const U k = stage_k[s];
+                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    if (uint64_t(g) < n) {
+                        if (dst_k) dst_k[g] = k;
+                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    }
                 }
             }
         }
@@ -440,7 +524,7 @@ __device__ __forceinline__ void copy_elems(const Control &c, uint64_t n) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_copy(const Control *__restrict__ ctrl, uint64_t n) {
+static __global__ void __launch_bounds__(256) k_copy(const Control *__restrict__ ctrl, uint64_t n) {
     const Control c = *ctrl;
     if (c.copy_mode == kCopyNone) return;
     switch (c.copy_elem_bytes) {

@@ -1,0 +1,150 @@
+// rsbd8g_launch.cuh - host-side launch sequence of one sort, templated on the key size; each
+// rsbd8g_sort_k*.cu instantiates it for one key size so the kernels compile in parallel.
+//
+//   memset(control, histograms, look-back state) -> histogram (or gather + histogram)
+//   -> plan (scan + pass-skip + ping-pong) -> one onesweep pass per digit -> copy step
+// all on the caller's stream, with no host synchronisation in between (a skipped pass returns at
+// once on the device), so the sequence can be captured in a CUDA graph.
+#pragma once
+#include <algorithm>
+#include <mutex>
+
+#include "rsbd8g_internal.h"
+#include "rsbd8g_kernels.cuh"
+
+namespace rsbd8g {
+
+constexpr int kHistThreads = 512;
+
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch, uint32_t dmask,
+                            cudaStream_t s) {
+    using SM = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
+    auto kern = k_onesweep<U, MODE, HAS_VAL, THREADS, ITEMS, S>;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static std::once_flag once[64];
+    static int occ[64];
+    std::call_once(once[dev & 63], [&] {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SM::kBytes));
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, THREADS, SM::kBytes);
+        occ[dev & 63] = b > 0 ? b : 1;
+    });
+    const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, uint64_t(occ[dev & 63]) * device_sms(dev)));
+    Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
+    const unsigned long long *bstart = reinterpret_cast<const unsigned long long *>(scratch + L.bstart);
+    for (uint32_t p = 0; p < passes; ++p) {
+        S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
+        LaunchTimer t(s, RSBD8G_KERNEL_ONESWEEP, uint32_t(sizeof(U)), p, n);
+        kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
+    }
+    return cudaGetLastError();
+}
+
+template <typename U, int MODE>
+cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, const Layout &L,
+                               unsigned char *scratch, uint32_t dmask, cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t per_cta = uint64_t(kHistThreads) * 64;   // keys per CTA sweep, to size the grid
+    const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per_cta - 1) / per_cta,
+                                                                            uint64_t(device_sms(dev)) * 4)));
+    unsigned long long *ghist = reinterpret_cast<unsigned long long *>(scratch + L.ghist);
+    LaunchTimer t(s, RSBD8G_KERNEL_HISTOGRAM, uint32_t(sizeof(U)), 0, n);
+    if (r.indirect) {
+        k_gather_histogram<U, MODE, kHistThreads><<<grid, kHistThreads, 0, s>>>(
+            static_cast<const uint64_t *>(in), n, dmask, r.off1, r.off2, int(r.indirect),
+            static_cast<const U *>(r.keys), reinterpret_cast<U *>(scratch + L.keys_a), ghist);
+    } else {
+        k_histogram<U, MODE, kHistThreads><<<grid, kHistThreads, 0, s>>>(static_cast<const U *>(in), n, dmask, ghist);
+    }
+    return cudaGetLastError();
+}
+
+#define RSBD8G_MODE_SWITCH(mode, CALL) \
+    switch (mode) {                    \
+        case 0: CALL(0); break;        \
+        case 1: CALL(1); break;        \
+        case 2: CALL(2); break;        \
+        case 3: CALL(3); break;        \
+        case 4: CALL(4); break;        \
+        case 5: CALL(5); break;        \
+        case 6: CALL(6); break;        \
+        default: CALL(7); break;       \
+    }
+
+template <typename U>
+cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in,
+                          void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
+    constexpr SweepGeometry gd = sweep_geometry(int(sizeof(U)), false);
+    constexpr SweepGeometry gi = sweep_geometry(int(sizeof(U)), true);
+    cudaError_t e;
+    {
+        LaunchTimer t(s, RSBD8G_KERNEL_MEMSET, uint32_t(sizeof(U)), 0, n);
+        e = cudaMemsetAsync(scratch, 0, L.zero_bytes, s);
+    }
+    if (e != cudaSuccess) return e;
+    const int mode = int(r.f.absv | (r.f.sign << 1) | (r.f.fltp << 2));
+    const uint32_t dmask = r.f.desc ? 0xFFu : 0u;
+#define RSBD8G_HIST(M) e = launch_histogram_t<U, M>(r, n, in, L, scratch, dmask, s)
+    RSBD8G_MODE_SWITCH(mode, RSBD8G_HIST)
+#undef RSBD8G_HIST
+    if (e != cudaSuccess) return e;
+    PlanArgs a{};
+    a.in = in;
+    a.out = out;
+    a.buf = buf;
+    a.keys_a = r.indirect ? scratch + L.keys_a : nullptr;
+    a.keys_b = r.indirect ? scratch + L.keys_b : nullptr;
+    a.elem_bytes = r.elem_bytes;
+    a.inplace = inplace;
+    a.to_buffer = to_buffer;
+    a.rev = r.rev;
+    a.indirect = r.indirect != 0;
+    a.passes = uint32_t(sizeof(U));
+    const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
+    a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
+    a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;
+    {
+        LaunchTimer t(s, RSBD8G_KERNEL_PLAN, uint32_t(sizeof(U)), 0, n);
+        k_plan<<<1, 256, 0, s>>>(reinterpret_cast<Control *>(scratch + L.ctrl),
+                                 reinterpret_cast<const unsigned long long *>(scratch + L.ghist),
+                                 reinterpret_cast<unsigned long long *>(scratch + L.bstart), n, a);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const uint32_t P = uint32_t(sizeof(U));
+    if (r.indirect) {
+        e = L.wide_status
+                ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, 0u, s)
+                : launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint32_t>(P, n, L, scratch, 0u, s);
+    } else if (L.wide_status) {
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint64_t>(P, n, L, scratch, dmask, s)
+        RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
+#undef RSBD8G_SWEEP
+    } else {
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint32_t>(P, n, L, scratch, dmask, s)
+        RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
+#undef RSBD8G_SWEEP
+    }
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint32_t cgrid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(device_sms(dev)) * 8)));
+    {
+        LaunchTimer t(s, RSBD8G_KERNEL_COPY, uint32_t(sizeof(U)), 0, n);
+        k_copy<<<cgrid, 256, 0, s>>>(reinterpret_cast<const Control *>(scratch + L.ctrl), n);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace rsbd8g
+
+#define RSBD8G_DEFINE_LAUNCH(name, U)                                                                          \
+    namespace rsbd8g {                                                                                         \
+    cudaError_t name(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in,   \
+                     void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {                    \
+        return launch_sort_t<U>(r, n, L, scratch, in, out, buf, inplace, to_buffer, s);                       \
+    }                                                                                                          \
+    }

@@ -1,0 +1,228 @@
+// facade_test.cpp - the rsbd8.hpp facade used the way the reference's portable unit test uses
+// the reference API (multiplatform/main.cpp), on device-resident arrays.  Known answers are
+// checked here; with an output directory argument the random cases are written as raw
+// files (inputs and outputs) for the Python test to compare with the oracle.
+#include <cuda_runtime_api.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rsbd8.hpp"
+
+static int failures = 0;
+#define CHECK(c)                                                                   \
+    do {                                                                           \
+        if (!(c)) {                                                                \
+            std::fprintf(stderr, "CHECK failed at line %d: %s\n", __LINE__, #c);   \
+            ++failures;                                                            \
+        }                                                                          \
+    } while (0)
+
+template <typename T>
+static T *todev(const std::vector<T> &h) {
+    T *d = nullptr;
+    cudaMalloc(reinterpret_cast<void **>(&d), h.size() * sizeof(T) + 1);
+    cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return d;
+}
+template <typename T>
+static std::vector<T> tohost(const T *d, std::size_t n) {
+    std::vector<T> h(n);
+    cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost);
+    return h;
+}
+
+enum cert_v_binencoding64 : std::uint8_t { e0 = 0, ei = 18, eq = 26, eB = 37, eE = 40, eU = 56, e_ = 63 };
+
+#pragma pack(push, 1)
+class Testmeclass {
+    std::uint64_t wasted{};
+    char misalignoffset{};
+
+public:
+    std::uint64_t co;
+    std::int64_t sco;
+    std::uint64_t get() const noexcept { return co; }
+    std::uint64_t getwparam(int testfor8in) const noexcept { return testfor8in == 8 ? co : 0; }
+    std::int64_t sget() const noexcept { return sco; }
+    Testmeclass(std::uint64_t input) noexcept : co{input}, sco{static_cast<std::int64_t>(input) - 1} {}
+};
+#pragma pack(pop)
+static_assert(sizeof(Testmeclass) == 25, "packed test class");
+
+struct Rec24 {
+    std::uint64_t id;
+    double key;
+    std::uint32_t tag;
+    std::uint32_t pad;
+};
+
+static std::uint64_t splitmix(std::uint64_t &s) {
+    std::uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+template <typename T>
+static void dump(const std::string &dir, const std::string &name, const std::vector<T> &v) {
+    if (dir.empty()) return;
+    FILE *f = std::fopen((dir + "/" + name).c_str(), "wb");
+    std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fclose(f);
+}
+
+int main(int argc, char **argv) {
+    const std::string outdir = argc > 1 ? argv[1] : "";
+    {  // multiplatform/main.cpp:10-19: uint32, in place
+        std::vector<std::uint32_t> h{18, 33, 21, 0, 5, 1, 13};
+        std::uint32_t *d = todev(h);
+        CHECK(rsbd8::radixsort(h.size(), d));
+        CHECK((tohost(d, h.size()) == std::vector<std::uint32_t>{0, 1, 5, 13, 18, 21, 33}));
+        cudaFree(d);
+    }
+    {  // multiplatform/main.cpp:191-198: single-byte enum, descending reverse and ascending
+        std::vector<cert_v_binencoding64> tein{e0, eB, e_, ei, eq, eU, eE};
+        auto *din = todev(tein);
+        cert_v_binencoding64 *dout = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), 7);
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::dscrevorder>(7, din, dout));
+        CHECK((tohost(dout, 7) == std::vector<cert_v_binencoding64>{e_, eU, eE, eB, eq, ei, e0}));
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::ascfwdorder>(7, din, dout));
+        CHECK((tohost(dout, 7) == std::vector<cert_v_binencoding64>{e0, ei, eq, eB, eE, eU, e_}));
+        cudaFree(din);
+        cudaFree(dout);
+    }
+    std::uint32_t *doutm = nullptr;
+    {  // multiplatform/main.cpp:201-205: float bit patterns, ascending
+        std::vector<std::uint32_t> inm{8, 0, 3, 1u << 31 | 2, 3, 1u << 31 | 18, 1u << 31 | 2};
+        auto *din = todev(inm);
+        cudaMalloc(reinterpret_cast<void **>(&doutm), 7 * 4);
+        CHECK(rsbd8::radixsortcopy(7, reinterpret_cast<float *>(din), reinterpret_cast<float *>(doutm)));
+        CHECK((tohost(doutm, 7) ==
+               std::vector<std::uint32_t>{1u << 31 | 18, 1u << 31 | 2, 1u << 31 | 2, 0, 3, 3, 8}));
+        cudaFree(din);
+    }
+    {  // multiplatform/main.cpp:208-215: float pointers, descending reverse order, ties by address
+        std::vector<float const *> inim{
+            reinterpret_cast<float const *>(doutm + 6), reinterpret_cast<float const *>(doutm + 3),
+            reinterpret_cast<float const *>(doutm + 4), reinterpret_cast<float const *>(doutm + 1),
+            reinterpret_cast<float const *>(doutm + 5), reinterpret_cast<float const *>(doutm),
+            reinterpret_cast<float const *>(doutm + 2)};
+        auto *din = todev(inim);
+        float const **dout = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), 7 * sizeof(void *));
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::dscrevorder>(7, din, dout));
+        auto o = tohost(dout, 7);
+        CHECK(o[0] == inim[0] && o[1] == inim[4] && o[2] == inim[2] && o[3] == inim[1] && o[4] == inim[6] &&
+              o[5] == inim[3] && o[6] == inim[5]);
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::ascfwdorder>(7, din, dout));
+        auto o2 = tohost(dout, 7);
+        std::vector<std::uint32_t> vals(7);
+        for (int i = 0; i < 7; ++i) cudaMemcpy(&vals[i], o2[i], 4, cudaMemcpyDeviceToHost);
+        CHECK((vals == std::vector<std::uint32_t>{1u << 31 | 18, 1u << 31 | 2, 1u << 31 | 2, 0, 3, 3, 8}));
+        cudaFree(din);
+        cudaFree(dout);
+    }
+    cudaFree(doutm);
+    {  // multiplatform/main.cpp:219-304: packed 25-byte class; getter, member and type+offset forms
+        Testmeclass *objs = nullptr;   // managed: the host evaluates getters, the device reads members
+        cudaMallocManaged(reinterpret_cast<void **>(&objs), 7 * sizeof(Testmeclass));
+        const std::uint64_t vals[7]{8, 0, 6, 4, 0, 2, 6};
+        for (int i = 0; i < 7; ++i) new (objs + i) Testmeclass(vals[i]);
+        std::vector<Testmeclass const *> fin;
+        for (int i = 0; i < 7; ++i) fin.push_back(objs + i);
+        auto *din = todev(fin);
+        Testmeclass const **dout = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), 7 * sizeof(void *));
+        const std::vector<int> want{1, 4, 5, 3, 2, 6, 0};
+        auto order = [&] {
+            auto o = tohost(dout, 7);
+            std::vector<int> idx;
+            for (auto p : o) idx.push_back(int(p - objs));
+            return idx;
+        };
+        CHECK((rsbd8::radixsortcopy<&Testmeclass::get>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<&Testmeclass::getwparam>(7, din, dout, 0, 8)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<&Testmeclass::co>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<std::uint64_t, 9>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<&Testmeclass::sget>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<&Testmeclass::sco>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<std::int64_t, 17>(7, din, dout)));
+        CHECK(order() == want);
+        CHECK((rsbd8::radixsortcopy<std::int64_t, 17, rsbd8::sortingdirection::dscrevorder>(7, din, dout)));
+        CHECK((order() == std::vector<int>{0, 6, 2, 3, 5, 4, 1}));
+        cudaFree(din);
+        cudaFree(dout);
+        cudaFree(objs);
+    }
+    {  // random cases for the oracle comparison: noalloc forms, modes, records by member
+        const std::size_t n = 100003;
+        std::uint64_t s = 12345;
+        std::vector<float> f(n);
+        for (auto &x : f) {
+            std::uint32_t b = std::uint32_t(splitmix(s));
+            if ((b & 63) == 0) b &= 0x80000000u;                 // +-0.0
+            std::memcpy(&x, &b, 4);
+        }
+        auto *din = todev(f);
+        float *dout = nullptr, *dbuf = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), n * 4);
+        cudaMalloc(reinterpret_cast<void **>(&dbuf), n * 4);
+        constexpr auto dsc = rsbd8::sortingdirection::dscrevorder;
+        constexpr auto abs = rsbd8::sortingmode::nativeabs;
+        void *scratch = nullptr;
+        cudaMalloc(&scratch, rsbd8::gpuscratchbytes<dsc, abs, float>(n));
+        rsbd8::radixsortcopynoalloc<dsc, abs>(n, 0u, nullptr, scratch, din, dout, dbuf);
+        CHECK(rsbd8g_scratch_status(scratch, nullptr) == RSBD8G_OK);
+        dump(outdir, "f32_in.bin", f);
+        dump(outdir, "f32_nativeabs_dscrevorder.bin", tohost(dout, n));
+        rsbd8::radixsortnoalloc<rsbd8::sortingdirection::ascrevorder>(n, scratch, din, dbuf, true);
+        cudaDeviceSynchronize();
+        dump(outdir, "f32_native_ascrevorder_movetobuffer.bin", tohost(dbuf, n));
+        cudaFree(din);
+        cudaFree(dout);
+        cudaFree(dbuf);
+        cudaFree(scratch);
+
+        std::vector<Rec24> recs(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            recs[i].id = i;
+            std::uint64_t b = splitmix(s);
+            recs[i].key = double(std::int64_t(b >> 11) - (std::int64_t(1) << 52)) / 1024.0;
+            if (i > 0 && (b & 7) == 0) recs[i].key = recs[b % i].key;
+        }
+        auto *drec = todev(recs);
+        std::vector<Rec24 *> ptrs(n);
+        for (std::size_t i = 0; i < n; ++i) ptrs[i] = drec + i;
+        auto *dp = todev(ptrs);
+        Rec24 **dpo = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dpo), n * sizeof(void *));
+        CHECK((rsbd8::radixsortcopy<&Rec24::key, rsbd8::sortingdirection::dscfwdorder>(n, dp, dpo)));
+        auto po = tohost(dpo, n);
+        std::vector<std::uint64_t> idx(n);
+        for (std::size_t i = 0; i < n; ++i) idx[i] = std::uint64_t(po[i] - drec);
+        std::vector<double> keys(n);
+        for (std::size_t i = 0; i < n; ++i) keys[i] = recs[i].key;
+        dump(outdir, "rec_keys.bin", keys);
+        dump(outdir, "rec_member_dscfwdorder_idx.bin", idx);
+        CHECK((rsbd8::radixsort<double, 8, rsbd8::sortingdirection::dscfwdorder>(n, dp)));
+        auto pi = tohost(dp, n);
+        for (std::size_t i = 0; i < n; ++i) CHECK_IDX: if (std::uint64_t(pi[i] - drec) != idx[i]) { ++failures; break; }
+        cudaFree(drec);
+        cudaFree(dp);
+        cudaFree(dpo);
+    }
+    std::printf("%s (%d failures)\n", failures ? "FAIL" : "PASS", failures);
+    return failures ? 1 : 0;
+}

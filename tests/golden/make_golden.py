@@ -7,7 +7,8 @@ has multithreading races: at some sizes it crashes or returns different orders f
 run to run.  A case is recorded as
   "ok"        both runs agree (the sha256 of the output bytes is stored),
   "crash"     a run died (signal / non-zero exit),
-  "unstable"  the runs disagree.
+  "unstable"  the runs disagree,
+  "hang"      a run did not finish within 60 s (the reference spins forever at some sizes).
 Inputs are regenerated from (generator, seed, n) with radixsortbidi8_gb300.synth, so the
 fixture stays small; outputs of n <= 64 are stored in full.
 """
@@ -109,8 +110,11 @@ def run_case(c: dict) -> bytes:
 
 
 def _spawn(c: dict) -> tuple[str, str | None, str | None]:
-    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--case", json.dumps(c)],
-                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    try:
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--case", json.dumps(c)],
+                           capture_output=True, text=True, timeout=60, cwd=ROOT)
+    except subprocess.TimeoutExpired:
+        return "hang", None, None
     if r.returncode != 0:
         return "crash", None, None
     line = r.stdout.strip().splitlines()[-1]
@@ -126,7 +130,12 @@ def main() -> None:
     cs = cases()
 
     def both(c):
-        r1, r2 = _spawn(c), _spawn(c)
+        r1 = _spawn(c)
+        if r1[0] == "hang":
+            return dict(c, status="hang")
+        r2 = _spawn(c)
+        if r2[0] == "hang":
+            return dict(c, status="hang")
         if r1[0] == "crash" or r2[0] == "crash":
             return dict(c, status="crash")
         if r1[1] != r2[1]:
@@ -138,6 +147,10 @@ def main() -> None:
 
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
         res = list(ex.map(both, cs))
+    # the reference races more under load: retry the failed cases one at a time
+    for i, r in enumerate(res):
+        if r["status"] != "ok":
+            res[i] = both(cs[i])
     with open(OUT, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "reference": "Radixsortbidi8.hpp (rsbd8)",
                    "cases": res}, f, indent=0)
