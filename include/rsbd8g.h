@@ -141,6 +141,24 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
                                                  void *input, void *buffer, int movetobuffer,
                                                  rsbd8g_stream stream);
 
+/* The plain-key copy sort (as rsbd8g_radixsortcopy, direct keys only) without any device
+ * allocation.  It has no counterpart in the reference: it exists for callers that must not
+ * call cudaMalloc -- plugins whose host framework owns all device memory through its own
+ * allocator or a fixed budget, latency-critical paths that cannot take cudaMalloc's implicit
+ * synchronisation, or callers that are only handed an input and an output buffer.
+ * The scratch and the ping-pong buffer live in one 64 MiB array in the library's device memory
+ * (one per GPU, kept until the process exits), so `count` is limited to what fits there:
+ * rsbd8g_scratch_bytes(count) + count * key_bytes rounded up to 256 bytes must not exceed
+ * 64 MiB -- about 53.6 M one-byte, 26.8 M two-byte, 13.4 M four-byte or 6.28 M eight-byte
+ * keys.  Larger counts return RSBD8G_ERR_TOO_LARGE without touching the device.
+ * The first call on a device looks up the array's device address (once per device), so make
+ * that first call before capturing the stream into a CUDA graph.  Every call reuses the same
+ * array and clears the parts that must start at zero; calls whose work overlaps on the GPU
+ * (other streams, other host threads) race on it, so order them.  Stream-ordered like the
+ * noalloc forms: read errors with a synchronising call of your own. */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_static(const rsbd8g_desc *desc, size_t count,
+                                                     const void *input, void *output, rsbd8g_stream stream);
+
 /* Wait for the stream, then read and clear the device-side status word of a
  * scratch area used by a noalloc call (RSBD8G_OK, RSBD8G_ERR_TIMEOUT, ...). */
 RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stream);
