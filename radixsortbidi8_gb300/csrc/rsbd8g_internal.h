@@ -59,7 +59,7 @@ struct SweepGeometry {
     int threads, items;
 };
 constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
-    return indirect ? SweepGeometry{256, 8} : SweepGeometry{256, key_bytes == 8 ? 12 : 16};
+    return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 12 : 16};
 }
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);

@@ -8,7 +8,7 @@
 //                                      pass-skip test, and the ping-pong plan of the passes
 //   k_onesweep                         one stable scatter pass of a surviving digit: persistent
 //                                      CTAs claim tiles in order, rank keys with a warp
-//                                      multisplit (__match_any_sync), resolve the tile's global
+//                                      multisplit (shared-memory match words), resolve the tile's global
 //                                      bucket offsets with a bounded decoupled look-back, stage the
 //                                      tile in shared memory sorted by digit and write it out
 //                                      coalesced
@@ -263,7 +263,8 @@ struct OnesweepSmem {
     static constexpr size_t kStageV = HAS_VAL ? size_t(kTile) * 8 : 0;
     static constexpr size_t kOffV = (kStageK + 15) & ~size_t(15);
     static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32 [WARPS][256]
-    static constexpr size_t kOffGofs = kOffWofs + size_t(kWarps) * kBuckets * 4;  // i64 [256]
+    static constexpr size_t kOffWmask = kOffWofs + size_t(kWarps) * kBuckets * 4; // u32 [WARPS][256]
+    static constexpr size_t kOffGofs = kOffWmask + size_t(kWarps) * kBuckets * 4; // i64 [256]
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;              // u64 [256]
     static constexpr size_t kOffMisc = kOffBstart + kBuckets * 8;              // u32 [16]
     static constexpr size_t kBytes = kOffMisc + 64;
@@ -276,26 +277,13 @@ __device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
     return (uint32_t(filter_key<MODE>(k) >> (pass * kRadixBits)) & (kBuckets - 1)) ^ dmask;
 }
 
-// peer mask of the lanes holding the same 8-bit digit (ballot per bit)
-__device__ __forceinline__ uint32_t match_digit(uint32_t d) {
-    uint32_t peers = 0xFFFFFFFFu;
-#pragma unroll
-    for (int k = 0; k < kRadixBits; ++k) {
-        const bool bit = (d >> k) & 1u;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, bit);
-        peers &= bit ? b : ~b;
-    }
-    return peers;
-}
-
-// resident CTAs per SM the register allocation is bounded for
-template <typename U, bool HAS_VAL>
+template <typename U, bool HAS_VAL, int THREADS>
 constexpr int onesweep_min_blocks() {
-    return HAS_VAL ? 3 : (sizeof(U) <= 4 ? 4 : 3);
+    return THREADS >= 512 ? 2 : (HAS_VAL ? 3 : (sizeof(U) <= 4 ? 4 : 3));
 }
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
-__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
+__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
     k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
                S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
@@ -324,6 +312,8 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
     uint32_t *wcnt = wofs + warp * kBuckets;   // this warp's digit counters, later its offsets
+    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask) + warp * kBuckets;
+    for (int i = lane; i < kBuckets; i += 32) wmask[i] = 0u;
     const uint32_t ltmask = lanemask_lt();
 
     for (;;) {
@@ -369,17 +359,23 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
             const uint32_t slot = slot0 + uint32_t(i) * 32u;
             dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
         }
-        // warp multisplit: peer masks first (independent), then the counter chain in slot order
-        uint32_t peers[ITEMS];
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) peers[i] = match_digit(dr[i]);
+        // warp multisplit in slot order: the lanes holding digit d OR their bit into the warp's mask
+        // word for d (a commutative update, so the mask is exact whatever order the lanes run in),
+        // read it back with the warp's running count of d, and the lowest lane of the group
+        // advances the count and clears the mask for the next item
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t d = dr[i];
+            atomicOr(wmask + d, 1u << lane);
+            __syncwarp();
+            const uint32_t peers = wmask[d];
             const uint32_t before = wcnt[d];
             __syncwarp();
-            const uint32_t lower = uint32_t(__popc(peers[i] & ltmask));
-            if (lower == 0) wcnt[d] = before + uint32_t(__popc(peers[i]));
+            const uint32_t lower = uint32_t(__popc(peers & ltmask));
+            if (lower == 0) {
+                wcnt[d] = before + uint32_t(__popc(peers));
+                wmask[d] = 0u;
+            }
             __syncwarp();
             dr[i] = ((before + lower) << 8) | d;
         }
@@ -415,7 +411,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
             const uint32_t ts = before + x - (count + (tid == kBuckets - 1 ? uint32_t(TILE) - tvalid : 0u));
 #pragma unroll
             for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * kBuckets + tid] += ts;
-            // decoupled look-back for digit tid: read predecessors four at a time (bounded wait)
+            // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
             uint64_t excl = 0;
             bool bad = false;
             if (tile > 0) {
@@ -424,12 +420,13 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
                 uint64_t t0 = 0;
                 bool done = false;
                 while (!done && j >= 0) {
-                    S w4[4];
+                    constexpr int kWin = 8;
+                    S w4[kWin];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q)
+                    for (int q = 0; q < kWin; ++q)
                         w4[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + tid) : S(0);
                     int q = 0;
-                    for (; q < 4 && j - q >= 0; ++q) {
+                    for (; q < kWin && j - q >= 0; ++q) {
                         const uint32_t st = StatusWord<S>::state(w4[q]);
                         if (st == kStInvalid) break;
                         excl += StatusWord<S>::value(w4[q]);
@@ -439,8 +436,8 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL>())
                         }
                     }
                     if (done) break;
-                    if (q == 4) {          // four aggregates: keep walking back
-                        j -= 4;
+                    if (q == kWin) {       // a window of aggregates: keep walking back
+                        j -= kWin;
                         continue;
                     }
                     j -= q;                // wait on the first unpublished predecessor
