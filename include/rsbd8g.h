@@ -159,8 +159,31 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
 RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_static(const rsbd8g_desc *desc, size_t count,
                                                      const void *input, void *output, rsbd8g_stream stream);
 
+/* ---- batched (segmented) sort -------------------------------------------------------------
+ * Many independent arrays of uneven sizes in one stream-ordered call: segment s is elements
+ * [offsets[s], offsets[s+1]) of `input` (offsets: a device array of nsegs + 1 non-decreasing
+ * uint64 values from 0 to total), sorted on its own, with the semantics of rsbd8g_radixsortcopy
+ * for desc (direct keys), into the same range of `output`.  Segments of at most the small
+ * cutoff are sorted whole in shared memory; larger ones run the onesweep passes, all of them
+ * in the same launches.  No host synchronisation happens inside, so the call can be captured
+ * into a CUDA graph and replayed.  Each segment must hold fewer than 2^30 keys (a device-side
+ * fault flag otherwise, read with rsbd8g_scratch_status).
+ * No counterpart in the reference (its callers loop over rsbd8::radixsortcopy per array). */
+typedef struct rsbd8g_segtuning {
+    uint32_t small_variant;   /* shape of the small-segment block sort: 0, 1 or 2 (threads x items of the block sort, per key size) */
+    uint32_t small_cutoff;    /* largest segment sorted whole in shared memory (0 = the shape's capacity) */
+    uint32_t reserved[2];
+} rsbd8g_segtuning;
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                        const rsbd8g_segtuning *tuning, size_t *bytes);
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                   const uint64_t *offsets, void *scratch, size_t scratch_bytes,
+                                                   const void *input, void *output, void *buffer,
+                                                   const rsbd8g_segtuning *tuning, rsbd8g_stream stream);
+
 /* Wait for the stream, then read and clear the device-side status word of a
- * scratch area used by a noalloc call (RSBD8G_OK, RSBD8G_ERR_TIMEOUT, ...). */
+ * scratch area used by a noalloc or segmented call (RSBD8G_OK, RSBD8G_ERR_TIMEOUT, ...). */
 RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stream);
 
 /* Human-readable name of a status code. */

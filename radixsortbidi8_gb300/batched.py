@@ -1,0 +1,205 @@
+"""Batched (segmented) sort: many independent arrays of uneven sizes in one stream-ordered call.
+
+``segmented_sortcopy`` sorts every segment ``[offsets[s], offsets[s+1])`` of a concatenated
+device array on its own (the semantics of ``radixsortcopy``); small segments are sorted whole in
+shared memory by a block-local radix sort, large ones run the onesweep passes, all in the same
+launches (C ABI ``rsbd8g_segmented_sortcopy``).  ``SegmentedSorter`` owns the buffers of one
+batch shape and can capture the whole call into a CUDA graph (one graph launch per batch).
+
+The small-segment block-sort shape (threads x items) and the small/large cutoff are picked per key
+size by ``autotune`` and kept in ``tuning.json`` beside this file; ``tuning_for`` reads it.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import api
+
+TUNING_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+SMALL_SHAPES = {  # variant -> (threads, items) per key size, as compiled in the library
+    1: [(256, 8), (256, 16), (512, 16)], 2: [(256, 8), (256, 16), (512, 16)],
+    4: [(256, 8), (256, 16), (512, 16)], 8: [(256, 8), (256, 12), (512, 12)],
+}
+
+
+class SegTuning(ctypes.Structure):
+    """rsbd8g_segtuning of include/rsbd8g.h"""
+    _fields_ = [("small_variant", ctypes.c_uint32), ("small_cutoff", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 2)]
+
+
+def _lib():
+    L = api.lib()
+    if not getattr(L, "_seg_sigs", False):
+        P, S, VP = ctypes.POINTER(api.Desc), ctypes.c_size_t, ctypes.c_void_p
+        L.rsbd8g_segmented_scratch_bytes.argtypes = [P, S, S, ctypes.POINTER(SegTuning), ctypes.POINTER(S)]
+        L.rsbd8g_segmented_scratch_bytes.restype = ctypes.c_int
+        L.rsbd8g_segmented_sortcopy.argtypes = [P, S, S, VP, VP, S, VP, VP, VP, ctypes.POINTER(SegTuning), VP]
+        L.rsbd8g_segmented_sortcopy.restype = ctypes.c_int
+        L._seg_sigs = True
+    return L
+
+
+def tuning_for(key_bytes: int) -> SegTuning:
+    """The tuned small-segment shape and cutoff for a key size (library defaults if untuned)."""
+    try:
+        with open(TUNING_PATH) as f:
+            t = json.load(f)["segmented"][str(key_bytes)]
+        return SegTuning(int(t["small_variant"]), int(t["small_cutoff"]))
+    except (OSError, KeyError, ValueError):
+        return SegTuning(1, 0)
+
+
+def segmented_scratch_bytes(key_dtype, total: int, nsegs: int, direction="ascfwdorder", mode="native",
+                            tuning: SegTuning | None = None) -> int:
+    d = api.make_desc(key_dtype, direction, mode)
+    t = tuning if tuning is not None else tuning_for(d.key_bytes)
+    out = ctypes.c_size_t(0)
+    api._check(_lib().rsbd8g_segmented_scratch_bytes(ctypes.byref(d), total, nsegs, ctypes.byref(t),
+                                                     ctypes.byref(out)), "rsbd8g_segmented_scratch_bytes")
+    return out.value
+
+
+def segmented_sortcopy(input, output, buffer, offsets, scratch, direction="ascfwdorder", mode="native",
+                       key_dtype=None, tuning: SegTuning | None = None, stream=None, flags: int = 0) -> None:
+    """Sort every segment of `input` into `output` (device tensors; `offsets` an int64/uint64 CUDA
+    tensor of nsegs + 1 offsets).  Stream-ordered; read device errors with api.scratch_status."""
+    d = api.make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode, flags=flags)
+    t = tuning if tuning is not None else tuning_for(d.key_bytes)
+    nsegs = int(offsets.numel()) - 1
+    api._check(_lib().rsbd8g_segmented_sortcopy(
+        ctypes.byref(d), int(input.numel()), nsegs, api._ptr(offsets), api._ptr(scratch),
+        scratch.numel() * scratch.element_size(), api._ptr(input), api._ptr(output), api._ptr(buffer),
+        ctypes.byref(t), api._stream(stream)), "rsbd8g_segmented_sortcopy")
+
+
+class SegmentedSorter:
+    """Buffers for one batch shape; ``run`` sorts, ``capture`` records one CUDA graph of the call
+    and ``replay`` launches it (one graph launch per batch)."""
+
+    def __init__(self, input, offsets, direction="ascfwdorder", mode="native", key_dtype=None,
+                 tuning: SegTuning | None = None, stream=None):
+        import torch
+        self.input, self.offsets = input, offsets
+        self.direction, self.mode = direction, mode
+        self.key_dtype = key_dtype if key_dtype is not None else input.dtype
+        self.tuning = tuning if tuning is not None else tuning_for(api.key_kind(self.key_dtype)[1])
+        self.output = torch.empty_like(input)
+        self.buffer = torch.empty_like(input)
+        nb = segmented_scratch_bytes(self.key_dtype, int(input.numel()), int(offsets.numel()) - 1,
+                                     direction, mode, self.tuning)
+        self.scratch = torch.empty(nb, dtype=torch.uint8, device=input.device)
+        self.stream = stream if stream is not None else torch.cuda.Stream(device=input.device)
+        self.graph = None
+
+    def run(self):
+        segmented_sortcopy(self.input, self.output, self.buffer, self.offsets, self.scratch, self.direction,
+                           self.mode, self.key_dtype, self.tuning, self.stream)
+        return self.output
+
+    def capture(self):
+        import torch
+        with torch.cuda.stream(self.stream):
+            self.run()                 # first call outside capture: kernel attributes, module loading
+            self.stream.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=self.stream):
+                self.run()
+        return self
+
+    def replay(self):
+        self.graph.replay()
+        return self.output
+
+    def status(self) -> int:
+        return api.scratch_status(self.scratch, self.stream)
+
+
+def sort_each(input, output, offsets_host: np.ndarray, direction="ascfwdorder", mode="native", key_dtype=None,
+              stream=None) -> None:
+    """The per-array loop the batched call replaces: one plain noalloc sort per segment."""
+    import torch
+    kd = key_dtype if key_dtype is not None else input.dtype
+    lens = np.diff(offsets_host)
+    big = int(lens.max()) if lens.size else 0
+    scratch = torch.empty(api.scratch_bytes(kd, max(big, 2), direction, mode), dtype=torch.uint8,
+                          device=input.device)
+    buf = torch.empty(max(big, 1), dtype=input.dtype, device=input.device)
+    es = input.element_size()
+    ip, op, bp = input.data_ptr(), output.data_ptr(), buf.data_ptr()
+    L = api.lib()
+    d = api.make_desc(kd, direction, mode)
+    st = api._stream(stream)
+    nb = scratch.numel()
+    sp = scratch.data_ptr()
+    for s in range(lens.size):
+        n = int(lens[s])
+        if n == 0:
+            continue
+        o = int(offsets_host[s]) * es
+        rc = L.rsbd8g_radixsortcopynoalloc(ctypes.byref(d), n, sp, nb, ip + o, op + o, bp, st)
+        if rc != 0:
+            raise api.RSBD8GError(rc, "radixsortcopynoalloc")
+
+
+# ---- autotuner -------------------------------------------------------------------------------
+
+def _synthetic_batch(key_bytes: int, nsegs: int, lo: int, hi: int, seed: int, device="cuda"):
+    import torch
+    from . import synth
+    lens = synth.log_uniform_lengths(seed, nsegs, lo, hi)
+    offs = np.zeros(nsegs + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    keys = synth.uniform_bits_torch(seed, int(offs[-1]), key_bytes, device=device)
+    return keys, torch.from_numpy(offs).to(device), offs
+
+
+def autotune(key_bytes_list=(2, 4, 8), nsegs: int = 20000, lo: int = 16, hi: int = 1 << 16, reps: int = 3,
+             write: bool = True) -> dict:
+    """Time every compiled small-segment shape and a few cutoffs on a synthetic log-uniform batch
+    per key size; keep the fastest in tuning.json."""
+    import torch
+    kd = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+    best = {}
+    report = {}
+    for kb in key_bytes_list:
+        keys, offs, _ = _synthetic_batch(kb, nsegs, lo, hi, seed=1234 + kb)
+        results = []
+        for v, (th, it) in enumerate(SMALL_SHAPES[kb]):
+            cap = th * it
+            for cutoff in sorted({cap // 4, cap // 2, cap}):
+                t = SegTuning(v, cutoff)
+                s = SegmentedSorter(keys, offs, key_dtype=kd[kb], tuning=t)
+                with torch.cuda.stream(s.stream):
+                    s.run()
+                    s.stream.synchronize()
+                    t0 = time.perf_counter()
+                    for _ in range(reps):
+                        s.run()
+                    s.stream.synchronize()
+                ms = (time.perf_counter() - t0) / reps * 1e3
+                results.append((ms, v, cutoff))
+                del s
+        results.sort()
+        ms, v, cutoff = results[0]
+        best[str(kb)] = {"small_variant": v, "small_cutoff": cutoff, "threads_items": SMALL_SHAPES[kb][v],
+                         "ms": round(ms, 3)}
+        report[str(kb)] = [{"ms": round(m, 3), "small_variant": vv, "small_cutoff": cc} for m, vv, cc in results]
+        del keys, offs
+    if write:
+        data = {}
+        try:
+            with open(TUNING_PATH) as f:
+                data = json.load(f)
+        except (OSError, ValueError):
+            pass
+        data.setdefault("segmented", {}).update(best)
+        data["segmented_workload"] = {"nsegs": nsegs, "lengths": f"log-uniform [{lo}, {hi}]", "reps": reps}
+        with open(TUNING_PATH, "w") as f:
+            json.dump(data, f, indent=1)
+    return {"best": best, "all": report}

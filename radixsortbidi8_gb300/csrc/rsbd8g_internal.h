@@ -62,6 +62,44 @@ constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
     return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 12 : 16};
 }
 
+#define RSBD8G_MODE_SWITCH(mode, CALL) \
+    switch (mode) {                    \
+        case 0: CALL(0); break;        \
+        case 1: CALL(1); break;        \
+        case 2: CALL(2); break;        \
+        case 3: CALL(3); break;        \
+        case 4: CALL(4); break;        \
+        case 5: CALL(5); break;        \
+        case 6: CALL(6); break;        \
+        default: CALL(7); break;       \
+    }
+
+// shapes of the small-segment block sort (threads x items = the largest small segment)
+struct SegSmallShape {
+    int threads, items;
+};
+constexpr SegSmallShape seg_small_shape(int key_bytes, int variant) {
+    return key_bytes == 8 ? (variant == 0 ? SegSmallShape{256, 8} : variant == 1 ? SegSmallShape{256, 12} : SegSmallShape{512, 12})
+                          : (variant == 0 ? SegSmallShape{256, 8} : variant == 1 ? SegSmallShape{256, 16} : SegSmallShape{512, 16});
+}
+constexpr int kSegSmallVariants = 3;
+
+// byte offsets of the parts of a segmented-sort scratch area
+struct SegLayout {
+    size_t ctrl, large_seg, large_tbase, small_seg, seg_hist, seg_mask, status, status_bytes, zero_bytes, total;
+    uint64_t nlarge_max, tiles_max;
+    uint32_t cutoff, small_variant, tile;
+};
+
+struct SegArgs;
+#define RSBD8G_DECLARE_SEG_LAUNCH(name)                                                                \
+    cudaError_t name(const Resolved &r, const SegArgs &a, const SegLayout &L, unsigned char *scratch, \
+                     const void *in, void *out, void *buf, cudaStream_t s);
+RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k1)
+RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k2)
+RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k4)
+RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k8)
+
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
 Layout layout_for(const Resolved &r, uint64_t n);
 rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,

@@ -282,221 +282,264 @@ constexpr int onesweep_min_blocks() {
     return THREADS >= 512 ? 2 : (HAS_VAL ? 3 : (sizeof(U) <= 4 ? 4 : 3));
 }
 
+// one tile of one scatter pass, relative to the array (or segment) it belongs to
+template <typename U, typename S>
+struct SweepTile {
+    const U *src_k;
+    U *dst_k;                 // null: keys are dropped (last pass of an indirect sort)
+    const uint64_t *src_v;
+    uint64_t *dst_v;
+    S *status;                // look-back words of tile 0 of this array / segment
+    uint64_t n;               // elements of the array / segment
+    uint32_t tile;            // tile index within the array / segment
+    bool reverse;             // read the source back to front
+};
+
+// Process one tile: load, rank (warp multisplit), publish and resolve the look-back, stage sorted
+// by digit in shared memory, write out.  `bstart` (shared) holds the bucket starts of this pass for
+// the array / segment.  Called by all threads; ends with a barrier.
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+__device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<U, S> &t,
+                                           const unsigned long long *bstart, int pass, uint32_t dmask,
+                                           uint32_t *err_word, uint32_t *abort_word, uint64_t spin_limit,
+                                           uint32_t stall_tile) {
+    using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
+    constexpr int TILE = L::kTile;
+    constexpr int WARPS = L::kWarps;
+    U *stage_k = reinterpret_cast<U *>(smem);
+    uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
+    uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
+    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..17] scan
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t *wcnt = wofs + warp * kBuckets;
+    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask) + warp * kBuckets;
+    const uint32_t ltmask = lanemask_lt();
+    const uint32_t tile = t.tile;
+    const uint64_t n = t.n;
+    const uint64_t tbase = uint64_t(tile) * TILE;
+    const uint32_t tvalid = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
+
+    // load ITEMS keys per thread, warp-striped: item i of lane l is slot w*32*ITEMS + i*32 + l.
+    // Slots past the end get digit 255: they rank after every real key of the tile.
+    U keys[ITEMS];
+    uint64_t vals[HAS_VAL ? ITEMS : 1];
+    uint32_t dr[ITEMS];      // digit, later (rank << 8) | digit
+    const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
+    if (!t.reverse && tvalid == TILE) {
+        const U *p = t.src_k + tbase + slot0;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+        if constexpr (HAS_VAL) {
+            const uint64_t *q = t.src_v + tbase + slot0;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 32];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t slot = slot0 + uint32_t(i) * 32u;
+            const uint64_t gi = tbase + slot;
+            const uint64_t si = t.reverse ? (n - 1u - gi) : gi;
+            const bool ok = slot < tvalid;
+            keys[i] = ok ? t.src_k[si] : U(~U(0));
+            if constexpr (HAS_VAL) vals[i] = ok ? t.src_v[si] : 0ull;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t slot = slot0 + uint32_t(i) * 32u;
+        dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
+    }
+    // warp multisplit in slot order: the lanes holding digit d OR their bit into the warp's mask
+    // word for d (a commutative update, so the mask is exact whatever order the lanes run in),
+    // read it back with the warp's running count of d, and the lowest lane of the group
+    // advances the count and clears the mask for the next item
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t d = dr[i];
+        atomicOr(wmask + d, 1u << lane);
+        __syncwarp();
+        const uint32_t peers = wmask[d];
+        const uint32_t before = wcnt[d];
+        __syncwarp();
+        const uint32_t lower = uint32_t(__popc(peers & ltmask));
+        if (lower == 0) {
+            wcnt[d] = before + uint32_t(__popc(peers));
+            wmask[d] = 0u;
+        }
+        __syncwarp();
+        dr[i] = ((before + lower) << 8) | d;
+    }
+    __syncthreads();
+
+    // per digit: exclusive offsets of the warps and the tile count; publish the aggregate
+    uint32_t count = 0, x = 0, run = 0;
+    if (tid < kBuckets) {
+#pragma unroll
+        for (int w2 = 0; w2 < WARPS; ++w2) {
+            const uint32_t c = wofs[w2 * kBuckets + tid];
+            wofs[w2 * kBuckets + tid] = run;
+            run += c;
+        }
+        count = run;
+        if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalid;   // the padding slots
+        if (tile != stall_tile)
+            st_relaxed(t.status + size_t(tile) * kBuckets + tid,
+                       StatusWord<S>::make(tile == 0 ? kStInclusive : kStAggregate, count));
+        x = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) misc[2 + warp] = x;
+    }
+    __syncthreads();
+    if (tid < kBuckets) {
+        uint32_t before = 0;
+        for (int i = 0; i < warp; ++i) before += misc[2 + i];
+        const uint32_t ts = before + x - run;          // tile start of digit tid
+#pragma unroll
+        for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * kBuckets + tid] += ts;
+        // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
+        uint64_t excl = 0;
+        bool bad = false;
+        if (tile > 0) {
+            int64_t j = int64_t(tile) - 1;
+            uint32_t spins = 0;
+            uint64_t t0 = 0;
+            bool done = false;
+            while (!done && j >= 0) {
+                constexpr int kWin = 8;
+                S w4[kWin];
+#pragma unroll
+                for (int q = 0; q < kWin; ++q)
+                    w4[q] = (j - q >= 0) ? ld_relaxed(t.status + size_t(j - q) * kBuckets + tid) : S(0);
+                int q = 0;
+                for (; q < kWin && j - q >= 0; ++q) {
+                    const uint32_t st = StatusWord<S>::state(w4[q]);
+                    if (st == kStInvalid) break;
+                    excl += StatusWord<S>::value(w4[q]);
+                    if (st == kStInclusive) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (done) break;
+                if (q == kWin) {       // a window of aggregates: keep walking back
+                    j -= kWin;
+                    continue;
+                }
+                j -= q;                // wait on the first unpublished predecessor
+                if (++spins > 16u) {
+                    if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
+                    const uint64_t now = globaltimer_ns();
+                    if (t0 == 0) t0 = now;
+                    else if (now - t0 > spin_limit) {
+                        atomicOr(err_word, kDevTimeout);
+                        atomicExch(abort_word, 1u);
+                        bad = true;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            if (tile != stall_tile)
+                st_relaxed(t.status + size_t(tile) * kBuckets + tid,
+                           StatusWord<S>::make(kStInclusive, excl + count));
+        }
+        if (bad) misc[1] = 1u;
+        gofs[tid] = (long long)(bstart[tid] + excl) - (long long)ts;
+    }
+    __syncthreads();
+    const bool tile_bad = misc[1] != 0 || tile == stall_tile;
+
+    // stage the tile in shared memory, sorted by digit (padding slots land past tvalid)
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t pos = wcnt[dr[i] & 0xFFu] + (dr[i] >> 8);
+        stage_k[pos] = keys[i];
+        if constexpr (HAS_VAL) stage_v[pos] = vals[i];
+    }
+    __syncthreads();
+    // write out: consecutive threads take consecutive slots of a bucket run
+    if (!tile_bad) {
+        if (tvalid == TILE) {
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
+                const U k = stage_k[s];
+                const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                if (uint64_t(g) < n) {
+                    if (t.dst_k) t.dst_k[g] = k;
+                    if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
+                }
+            }
+        } else {
+            for (uint32_t s = tid; s < tvalid; s += THREADS) {
+                const U k = stage_k[s];
+                const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                if (uint64_t(g) < n) {
+                    if (t.dst_k) t.dst_k[g] = k;
+                    if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+__device__ __forceinline__ void sweep_init_smem(unsigned char *smem) {
+    using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
+    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
+    for (int i = threadIdx.x; i < L::kWarps * kBuckets; i += THREADS) {
+        wmask[i] = 0u;
+        wofs[i] = 0u;
+    }
+}
+
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
     k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
                S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
-    constexpr int TILE = L::kTile;
-    constexpr int WARPS = L::kWarps;
     static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
-    static_assert(TILE <= 65535, "tile ranks are 16-bit");
+    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     extern __shared__ __align__(16) unsigned char smem[];
-    U *stage_k = reinterpret_cast<U *>(smem);
-    uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
-    uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
-    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
-    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [0] tile [1] bad [2..9] scan
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);
 
     const PassPlan plan = ctrl->plan[pass];
     if (!plan.active) return;
-    const U *__restrict__ src_k = static_cast<const U *>(plan.src_keys);
-    U *__restrict__ dst_k = static_cast<U *>(plan.dst_keys);
-    const uint64_t *__restrict__ src_v = static_cast<const uint64_t *>(plan.src_vals);
-    uint64_t *__restrict__ dst_v = static_cast<uint64_t *>(plan.dst_vals);
-    const bool reverse = plan.reverse != 0;
+    SweepTile<U, S> t;
+    t.src_k = static_cast<const U *>(plan.src_keys);
+    t.dst_k = static_cast<U *>(plan.dst_keys);
+    t.src_v = static_cast<const uint64_t *>(plan.src_vals);
+    t.dst_v = static_cast<uint64_t *>(plan.dst_vals);
+    t.status = status;
+    t.n = n;
+    t.reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
-    uint32_t *wcnt = wofs + warp * kBuckets;   // this warp's digit counters, later its offsets
-    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask) + warp * kBuckets;
-    for (int i = lane; i < kBuckets; i += 32) wmask[i] = 0u;
-    const uint32_t ltmask = lanemask_lt();
-
+    for (int i = threadIdx.x; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
+    sweep_init_smem<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem);
     for (;;) {
-        if (tid == 0) {
+        if (threadIdx.x == 0) {
             misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
             misc[1] = 0;
         }
-        for (int i = lane; i < kBuckets; i += 32) wcnt[i] = 0;
         __syncthreads();
         const uint32_t tile = misc[0];
         if (tile >= num_tiles) break;
-        const uint64_t tbase = uint64_t(tile) * TILE;
-        const uint32_t tvalid = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
-
-        // load ITEMS keys per thread, warp-striped: item i of lane l is slot w*32*ITEMS + i*32 + l.
-        // Slots past the end get digit 255: they rank after every real key of the tile.
-        U keys[ITEMS];
-        uint64_t vals[HAS_VAL ? ITEMS : 1];
-        uint32_t dr[ITEMS];      // digit, later (rank << 8) | digit
-        const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
-        if (!reverse && tvalid == TILE) {
-            const U *p = src_k + tbase + slot0;
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
-            if constexpr (HAS_VAL) {
-                const uint64_t *q = src_v + tbase + slot0;
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 32];
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t slot = slot0 + uint32_t(i) * 32u;
-                const uint64_t gi = tbase + slot;
-                const uint64_t si = reverse ? (n - 1u - gi) : gi;
-                const bool ok = slot < tvalid;
-                keys[i] = ok ? src_k[si] : U(~U(0));
-                if constexpr (HAS_VAL) vals[i] = ok ? src_v[si] : 0ull;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t slot = slot0 + uint32_t(i) * 32u;
-            dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
-        }
-        // warp multisplit in slot order: the lanes holding digit d OR their bit into the warp's mask
-        // word for d (a commutative update, so the mask is exact whatever order the lanes run in),
-        // read it back with the warp's running count of d, and the lowest lane of the group
-        // advances the count and clears the mask for the next item
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t d = dr[i];
-            atomicOr(wmask + d, 1u << lane);
-            __syncwarp();
-            const uint32_t peers = wmask[d];
-            const uint32_t before = wcnt[d];
-            __syncwarp();
-            const uint32_t lower = uint32_t(__popc(peers & ltmask));
-            if (lower == 0) {
-                wcnt[d] = before + uint32_t(__popc(peers));
-                wmask[d] = 0u;
-            }
-            __syncwarp();
-            dr[i] = ((before + lower) << 8) | d;
-        }
-        __syncthreads();
-
-        // per digit: exclusive offsets of the warps and the tile count; publish the aggregate
-        uint32_t count = 0, x = 0;
-        if (tid < kBuckets) {
-            uint32_t run = 0;
-#pragma unroll
-            for (int w2 = 0; w2 < WARPS; ++w2) {
-                const uint32_t c = wofs[w2 * kBuckets + tid];
-                wofs[w2 * kBuckets + tid] = run;
-                run += c;
-            }
-            count = run;
-            if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalid;   // the padding slots
-            if (tile != stall_tile)
-                st_relaxed(status + size_t(tile) * kBuckets + tid,
-                           StatusWord<S>::make(tile == 0 ? kStInclusive : kStAggregate, count));
-            x = run;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                if (lane >= o) x += y;
-            }
-            if (lane == 31) misc[2 + warp] = x;
-        }
-        __syncthreads();
-        if (tid < kBuckets) {
-            uint32_t before = 0;
-            for (int i = 0; i < warp; ++i) before += misc[2 + i];
-            const uint32_t ts = before + x - (count + (tid == kBuckets - 1 ? uint32_t(TILE) - tvalid : 0u));
-#pragma unroll
-            for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * kBuckets + tid] += ts;
-            // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
-            uint64_t excl = 0;
-            bool bad = false;
-            if (tile > 0) {
-                int64_t j = int64_t(tile) - 1;
-                uint32_t spins = 0;
-                uint64_t t0 = 0;
-                bool done = false;
-                while (!done && j >= 0) {
-                    constexpr int kWin = 8;
-                    S w4[kWin];
-#pragma unroll
-                    for (int q = 0; q < kWin; ++q)
-                        w4[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + tid) : S(0);
-                    int q = 0;
-                    for (; q < kWin && j - q >= 0; ++q) {
-                        const uint32_t st = StatusWord<S>::state(w4[q]);
-                        if (st == kStInvalid) break;
-                        excl += StatusWord<S>::value(w4[q]);
-                        if (st == kStInclusive) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (done) break;
-                    if (q == kWin) {       // a window of aggregates: keep walking back
-                        j -= kWin;
-                        continue;
-                    }
-                    j -= q;                // wait on the first unpublished predecessor
-                    if (++spins > 16u) {
-                        if (*reinterpret_cast<volatile uint32_t *>(&ctrl->abort)) { bad = true; break; }
-                        const uint64_t now = globaltimer_ns();
-                        if (t0 == 0) t0 = now;
-                        else if (now - t0 > spin_limit) {
-                            atomicOr(&ctrl->error, kDevTimeout);
-                            atomicExch(&ctrl->abort, 1u);
-                            bad = true;
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
-                if (tile != stall_tile)
-                    st_relaxed(status + size_t(tile) * kBuckets + tid,
-                               StatusWord<S>::make(kStInclusive, excl + count));
-            }
-            if (bad) misc[1] = 1u;
-            gofs[tid] = (long long)(bstart[tid] + excl) - (long long)ts;
-        }
-        __syncthreads();
-        const bool tile_bad = misc[1] != 0 || tile == stall_tile;
-
-        // stage the tile in shared memory, sorted by digit (padding slots land past tvalid)
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t pos = wcnt[dr[i] & 0xFFu] + (dr[i] >> 8);
-            stage_k[pos] = keys[i];
-            if constexpr (HAS_VAL) stage_v[pos] = vals[i];
-        }
-        __syncthreads();
-        // write out: consecutive threads take consecutive slots of a bucket run
-        if (!tile_bad) {
-            if (tvalid == TILE) {
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
-                    const U k = stage_k[s];
-                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
-                    if (uint64_t(g) < n) {
-                        if (dst_k) dst_k[g] = k;
-                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
-                    }
-                }
-            } else {
-                for (uint32_t s = tid; s < tvalid; s += THREADS) {
-                    const U k = stage_k[s];
-                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
-                    if (uint64_t(g) < n) {
-                        if (dst_k) dst_k[g] = k;
-                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
-                    }
-                }
-            }
-        }
-        __syncthreads();
+        t.tile = tile;
+        sweep_tile<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem, t, bstart, pass, dmask, &ctrl->error, &ctrl->abort,
+                                                        spin_limit, stall_tile);
+        // sweep_tile leaves the warp counters holding offsets: zero them for the next tile
+        uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
+        for (int i = threadIdx.x; i < L::kWarps * kBuckets; i += THREADS) wofs[i] = 0u;
     }
 }
 

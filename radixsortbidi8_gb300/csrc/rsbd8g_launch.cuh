@@ -63,18 +63,6 @@ cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, co
     return cudaGetLastError();
 }
 
-#define RSBD8G_MODE_SWITCH(mode, CALL) \
-    switch (mode) {                    \
-        case 0: CALL(0); break;        \
-        case 1: CALL(1); break;        \
-        case 2: CALL(2); break;        \
-        case 3: CALL(3); break;        \
-        case 4: CALL(4); break;        \
-        case 5: CALL(5); break;        \
-        case 6: CALL(6); break;        \
-        default: CALL(7); break;       \
-    }
-
 template <typename U>
 cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in,
                           void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {

@@ -1,0 +1,388 @@
+// rsbd8g_segmented.cuh - batched (segmented) sort: many independent arrays of uneven sizes in one
+// stream-ordered launch sequence without host synchronisation (capturable as one CUDA graph).
+//
+// Segment s is [offsets[s], offsets[s+1]) of the concatenated input; every segment is sorted on
+// its own with the semantics of the plain sort (Radixsortbidi8.hpp rsbd8::radixsortcopy).
+//   k_seg_classify   small (<= cutoff keys) or large; compacts both lists on the device
+//   k_seg_small      persistent CTAs sort each small segment whole in shared memory: a block-local
+//                    LSD radix sort over 8-bit digits with the same warp multisplit and the
+//                    reference's pass-skip test per segment
+//   k_seg_hist       per large segment, all digit histograms in one read (tiles in order)
+//   k_seg_plan       per large segment: exclusive scans, pass-skip mask
+//   k_seg_sweep      one onesweep pass over the tiles of every large segment: look-back chains
+//                    stay inside a segment; each segment ping-pongs by its own surviving passes
+//   k_seg_copy       large segments whose every digit was skipped (plain or reversed copy)
+#pragma once
+#include "rsbd8g_kernels.cuh"
+
+namespace rsbd8g {
+
+struct SegControl {
+    uint32_t error;
+    uint32_t abort;
+    uint32_t nlarge;
+    uint32_t nsmall;
+    uint32_t ntiles;          // tiles of all large segments
+    uint32_t small_counter;
+    uint32_t tile_counter[kMaxPasses];
+    uint64_t spin_limit_ns;
+    uint32_t pad[4];
+};
+
+struct SegArgs {
+    const uint64_t *offsets;  // nsegs + 1
+    uint64_t total;           // elements of the concatenated arrays
+    uint32_t nsegs;
+    uint32_t cutoff;          // largest small segment
+    uint32_t tile;            // keys per onesweep tile
+    uint32_t rev;
+    uint32_t dmask;
+    uint32_t nlarge_max;
+    SegControl *ctrl;
+    uint32_t *large_seg;      // [nlarge_max]
+    uint32_t *large_tbase;    // [nlarge_max + 1]
+    uint32_t *small_seg;      // [nsegs]
+    uint32_t *seg_hist;       // [nlarge_max][P][256]: counts, then bucket starts
+    uint32_t *seg_mask;       // [nlarge_max]: surviving digits
+};
+
+__device__ __forceinline__ uint64_t seg_len(const uint64_t *off, uint32_t s) { return off[s + 1] - off[s]; }
+
+// one CTA of 1024 threads classifies every segment; a single 64-bit atomic per warp hands out
+// (list index, tile base) pairs so tile bases grow with the list index
+static __global__ void __launch_bounds__(1024) k_seg_classify(SegArgs a) {
+    SegControl *c = a.ctrl;
+    __shared__ unsigned long long large_ctr;   // (count << 32) | tiles
+    __shared__ uint32_t small_ctr;
+    __shared__ uint32_t too_long;
+    if (threadIdx.x == 0) {
+        large_ctr = 0;
+        small_ctr = 0;
+        too_long = 0;
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = 0; base < a.nsegs; base += blockDim.x) {
+        const uint32_t s = base + threadIdx.x;
+        const bool ok = s < a.nsegs;
+        const uint64_t len = ok ? seg_len(a.offsets, s) : 0;
+        if (len >= (uint64_t(1) << 30)) too_long = 1u;
+        const bool large = ok && len > a.cutoff;
+        const bool small = ok && !large && len > 0;
+        const uint32_t tiles = large ? uint32_t((len + a.tile - 1) / a.tile) : 0u;
+        // warp-aggregated reservation of list slots and tiles
+        const uint32_t lmask = __ballot_sync(0xFFFFFFFFu, large);
+        uint32_t tsum = tiles, tpre;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, tsum, o);
+            if (lane >= uint32_t(o)) tsum += y;
+        }
+        tpre = tsum - tiles;
+        const uint32_t ttot = __shfl_sync(0xFFFFFFFFu, tsum, 31);
+        unsigned long long old = 0;
+        if (lane == 0 && lmask)
+            old = atomicAdd(&large_ctr, (uint64_t(__popc(lmask)) << 32) | uint64_t(ttot));
+        old = __shfl_sync(0xFFFFFFFFu, old, 0);
+        if (large) {
+            const uint32_t idx = uint32_t(old >> 32) + uint32_t(__popc(lmask & lanemask_lt()));
+            if (idx < a.nlarge_max) {
+                a.large_seg[idx] = s;
+                a.large_tbase[idx] = uint32_t(old) + tpre;
+            } else {
+                too_long = 1u;      // more large segments than the layout holds: inconsistent offsets
+            }
+        }
+        const uint32_t smask = __ballot_sync(0xFFFFFFFFu, small);
+        uint32_t sold = 0;
+        if (lane == 0 && smask) sold = atomicAdd(&small_ctr, uint32_t(__popc(smask)));
+        sold = __shfl_sync(0xFFFFFFFFu, sold, 0);
+        if (small) a.small_seg[sold + uint32_t(__popc(smask & lanemask_lt()))] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // offsets must start at 0 and end at or before `total` (then, being non-decreasing, every
+        // segment lies inside the arrays; a decreasing pair shows up as a huge length above)
+        if (a.offsets[0] != 0 || a.offsets[a.nsegs] > a.total) too_long = 1u;
+        c->nlarge = min(uint32_t(large_ctr >> 32), a.nlarge_max);
+        c->ntiles = uint32_t(large_ctr);
+        a.large_tbase[c->nlarge] = c->ntiles;
+        if (too_long) {
+            c->nlarge = 0;
+            c->nsmall = 0;
+            c->ntiles = 0;
+        }
+        if (!too_long) c->nsmall = small_ctr;
+        if (too_long) {
+            c->error |= kDevFault;
+            c->abort = 1u;
+        }
+    }
+}
+
+// index of the large segment owning global tile gt (tile bases are non-decreasing)
+__device__ __forceinline__ uint32_t seg_of_tile(const uint32_t *tbase, uint32_t nlarge, uint32_t gt) {
+    uint32_t lo = 0, hi = nlarge;            // invariant: tbase[lo] <= gt < tbase[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (tbase[mid] <= gt) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// all digit histograms of every large segment; CTA c reads a contiguous run of tiles in order
+template <typename U, int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__restrict__ in) {
+    constexpr int P = int(sizeof(U));
+    __shared__ uint32_t sh[P * kBuckets];
+    const SegControl *c = a.ctrl;
+    if (c->abort) return;
+    const uint32_t T = c->ntiles, nl = c->nlarge;
+    if (T == 0) return;
+    const uint32_t t0 = uint32_t(uint64_t(T) * blockIdx.x / gridDim.x);
+    const uint32_t t1 = uint32_t(uint64_t(T) * (blockIdx.x + 1) / gridDim.x);
+    if (t0 >= t1) return;
+    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) sh[i] = 0;
+    __syncthreads();
+    uint32_t idx = seg_of_tile(a.large_tbase, nl, t0);
+    for (uint32_t gt = t0; gt < t1;) {
+        while (a.large_tbase[idx + 1] <= gt) ++idx;
+        const uint32_t seg = a.large_seg[idx];
+        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
+        const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
+        const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
+        const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint64_t b = k0 + (threadIdx.x & ~31u); b < k1; b += THREADS) {
+            const uint64_t i = b + lane;
+            const bool ok = i < k1;
+            count_key(sh, filter_key<MODE>(ok ? in[s0 + i] : U(0)), ok, a.dmask);
+        }
+        __syncthreads();
+        uint32_t *gh = a.seg_hist + size_t(idx) * P * kBuckets;
+        for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
+            const uint32_t v = sh[i];
+            if (v) atomicAdd(gh + i, v);
+            sh[i] = 0;
+        }
+        __syncthreads();
+        gt = tend;
+    }
+}
+
+// per large segment (one CTA each): bucket starts in place of the counts, surviving-digit mask
+static __global__ void __launch_bounds__(256) k_seg_plan(SegArgs a, int passes) {
+    const SegControl *c = a.ctrl;
+    if (c->abort) return;
+    __shared__ uint32_t wsum[8];
+    const uint32_t nl = c->nlarge;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    for (uint32_t idx = blockIdx.x; idx < nl; idx += gridDim.x) {
+        const uint32_t seg = a.large_seg[idx];
+        const uint64_t len = seg_len(a.offsets, seg);
+        uint32_t mask = 0;
+        for (int p = 0; p < passes; ++p) {
+            uint32_t *h = a.seg_hist + (size_t(idx) * passes + p) * kBuckets;
+            const uint32_t v = h[t];
+            const int skip = __syncthreads_or(uint64_t(v) == len);
+            uint32_t x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) wsum[w] = x;
+            __syncthreads();
+            uint32_t before = 0;
+            for (int i = 0; i < w; ++i) before += wsum[i];
+            h[t] = before + x - v;
+            if (!skip) mask |= 1u << p;
+            __syncthreads();
+        }
+        if (t == 0) a.seg_mask[idx] = mask;
+    }
+}
+
+// one onesweep pass over the tiles of every large segment
+template <typename U, int MODE, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS>())
+    k_seg_sweep(SegArgs a, int pass, int passes, const U *__restrict__ in, U *__restrict__ out,
+                U *__restrict__ buf, uint32_t *__restrict__ status, uint32_t stall_tile) {
+    using L = OnesweepSmem<U, false, THREADS, ITEMS>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);
+    SegControl *c = a.ctrl;
+    if (c->abort) return;
+    const uint32_t T = c->ntiles, nl = c->nlarge;
+    const uint64_t spin_limit = c->spin_limit_ns;
+    sweep_init_smem<U, MODE, false, THREADS, ITEMS, uint32_t>(smem);
+    for (;;) {
+        if (threadIdx.x == 0) {
+            misc[0] = atomicAdd(&c->tile_counter[pass], 1u);
+            misc[1] = 0;
+        }
+        __syncthreads();
+        const uint32_t gt = misc[0];
+        if (gt >= T) break;
+        const uint32_t idx = seg_of_tile(a.large_tbase, nl, gt);
+        const uint32_t mask = a.seg_mask[idx];
+        if (!((mask >> pass) & 1u)) {        // this digit is skipped for the segment
+            __syncthreads();
+            continue;
+        }
+        const uint32_t seg = a.large_seg[idx];
+        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
+        const int k = __popc(mask), i = __popc(mask & ((1u << pass) - 1u)) + 1;
+        const U *src = (i == 1) ? in : (((k - (i - 1)) % 2 == 0) ? out : buf);
+        U *dst = ((k - i) % 2 == 0) ? out : buf;
+        const uint32_t *bs = a.seg_hist + (size_t(idx) * passes + pass) * kBuckets;
+        for (int j = threadIdx.x; j < kBuckets; j += THREADS) bstart[j] = bs[j];
+        SweepTile<U, uint32_t> t;
+        t.src_k = src + s0;
+        t.dst_k = dst + s0;
+        t.src_v = nullptr;
+        t.dst_v = nullptr;
+        t.status = status + size_t(a.large_tbase[idx]) * kBuckets;
+        t.n = len;
+        t.tile = gt - a.large_tbase[idx];
+        t.reverse = a.rev && i == 1;
+        sweep_tile<U, MODE, false, THREADS, ITEMS, uint32_t>(smem, t, bstart, pass, a.dmask, &c->error, &c->abort,
+                                                             spin_limit, stall_tile);
+        uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
+        for (int j = threadIdx.x; j < L::kWarps * kBuckets; j += THREADS) wofs[j] = 0u;
+    }
+}
+
+// large segments with every digit skipped: plain or reversed copy (one warp per segment)
+template <typename U>
+__global__ void __launch_bounds__(256) k_seg_copy(SegArgs a, const U *__restrict__ in, U *__restrict__ out) {
+    const SegControl *c = a.ctrl;
+    if (c->abort) return;
+    const uint32_t nl = c->nlarge;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < nl; idx += (gridDim.x * blockDim.x) >> 5) {
+        if (a.seg_mask[idx]) continue;
+        const uint32_t seg = a.large_seg[idx];
+        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
+        for (uint64_t i = lane; i < len; i += 32) out[s0 + i] = in[s0 + (a.rev ? len - 1 - i : i)];
+    }
+}
+
+// ---- small segments: whole-segment LSD radix sort in shared memory ----------------------------
+
+template <typename U, int THREADS, int ITEMS>
+struct SmallSmem {
+    static constexpr int kCap = THREADS * ITEMS;
+    static constexpr int kWarps = THREADS / 32;
+    static constexpr int kStride = kBuckets + 1;                 // + one bucket for idle lanes
+    static constexpr size_t kOffB = (size_t(kCap) * sizeof(U) + 15) & ~size_t(15);
+    static constexpr size_t kOffR = kOffB + ((size_t(kCap) * sizeof(U) + 15) & ~size_t(15));
+    static constexpr size_t kOffWofs = kOffR + size_t(kCap) * 4;
+    static constexpr size_t kOffWmask = kOffWofs + size_t(kWarps) * kStride * 4;
+    static constexpr size_t kOffMisc = kOffWmask + size_t(kWarps) * kStride * 4;
+    static constexpr size_t kBytes = kOffMisc + 64;
+};
+
+template <typename U, int MODE, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__restrict__ in, U *__restrict__ out) {
+    using L = SmallSmem<U, THREADS, ITEMS>;
+    constexpr int P = int(sizeof(U));
+    constexpr int WARPS = L::kWarps;
+    constexpr int ST = L::kStride;
+    static_assert(THREADS >= kBuckets, "one thread per digit");
+    extern __shared__ __align__(16) unsigned char smem[];
+    U *A = reinterpret_cast<U *>(smem);
+    U *B = reinterpret_cast<U *>(smem + L::kOffB);
+    uint32_t *R = reinterpret_cast<uint32_t *>(smem + L::kOffR);
+    uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
+    uint32_t *wmaskall = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] job [1] skip [2..9] scan
+    SegControl *c = a.ctrl;
+    if (c->abort) return;
+    const uint32_t ns = c->nsmall;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t *wcnt = wofs + warp * ST;
+    uint32_t *wmask = wmaskall + warp * ST;
+    const uint32_t ltmask = lanemask_lt();
+    for (int i = tid; i < WARPS * ST; i += THREADS) wmaskall[i] = 0u;
+    for (;;) {
+        if (tid == 0) misc[0] = atomicAdd(&c->small_counter, 1u);
+        __syncthreads();
+        const uint32_t job = misc[0];
+        if (job >= ns) break;
+        const uint32_t seg = a.small_seg[job];
+        const uint64_t s0 = a.offsets[seg];
+        const uint32_t len = uint32_t(a.offsets[seg + 1] - s0);
+        for (uint32_t i = tid; i < len; i += THREADS) A[i] = in[s0 + (a.rev ? len - 1u - i : i)];
+        // warp w ranks slots [w * chunk, min((w + 1) * chunk, len)) in steps of 32
+        const uint32_t chunk = ((len + WARPS - 1) / WARPS + 31u) & ~31u;
+        const uint32_t w0 = min(len, uint32_t(warp) * chunk), w1 = min(len, w0 + chunk);
+        U *src = A, *dst = B;
+        for (int p = 0; p < P; ++p) {
+            for (int i = lane; i < ST; i += 32) wcnt[i] = 0u;
+            if (tid == 0) misc[1] = 0u;
+            __syncthreads();
+            for (uint32_t b = w0; b < w1; b += 32) {
+                const uint32_t slot = b + uint32_t(lane);
+                const bool ok = slot < w1;
+                const uint32_t d = ok ? pass_digit<MODE>(src[slot], p, a.dmask) : uint32_t(kBuckets);
+                atomicOr(wmask + d, 1u << lane);
+                __syncwarp();
+                const uint32_t peers = wmask[d];
+                const uint32_t before = wcnt[d];
+                __syncwarp();
+                const uint32_t lower = uint32_t(__popc(peers & ltmask));
+                if (lower == 0) {
+                    wcnt[d] = before + uint32_t(__popc(peers));
+                    wmask[d] = 0u;
+                }
+                __syncwarp();
+                if (ok) R[slot] = ((before + lower) << 8) | d;
+            }
+            __syncthreads();
+            uint32_t run = 0, x = 0;
+            if (tid < kBuckets) {
+#pragma unroll
+                for (int w2 = 0; w2 < WARPS; ++w2) {
+                    const uint32_t cc = wofs[w2 * ST + tid];
+                    wofs[w2 * ST + tid] = run;
+                    run += cc;
+                }
+                if (run == len) misc[1] = 1u;        // pass-skip: one bucket holds every key
+                x = run;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) misc[2 + warp] = x;
+            }
+            __syncthreads();
+            const bool skip = misc[1] != 0;
+            if (tid < kBuckets && !skip) {
+                uint32_t before = 0;
+                for (int i = 0; i < warp; ++i) before += misc[2 + i];
+                const uint32_t ts = before + x - run;
+#pragma unroll
+                for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * ST + tid] += ts;
+            }
+            __syncthreads();
+            if (!skip) {
+                for (uint32_t slot = w0 + uint32_t(lane); slot < w1; slot += 32) {
+                    const uint32_t v = R[slot];
+                    dst[wcnt[v & 0xFFu] + (v >> 8)] = src[slot];
+                }
+                U *tmp = src;
+                src = dst;
+                dst = tmp;
+            }
+            __syncthreads();
+        }
+        for (uint32_t i = tid; i < len; i += THREADS) out[s0 + i] = src[i];
+        __syncthreads();
+    }
+}
+
+}  // namespace rsbd8g

@@ -1,0 +1,117 @@
+// rsbd8g_segmented_api.cu - C ABI of the batched (segmented) sort declared in include/rsbd8g.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "rsbd8g.h"
+#include "rsbd8g_internal.h"
+#include "rsbd8g_segmented.cuh"
+
+namespace rsbd8g {
+namespace {
+
+constexpr size_t kA = 256;
+constexpr size_t up(size_t x) { return (x + kA - 1) & ~(kA - 1); }
+
+rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, const rsbd8g_segtuning *t,
+                         SegLayout *L) {
+    *L = SegLayout{};
+    const uint32_t variant = t ? t->small_variant : 1u;
+    if (variant >= uint32_t(kSegSmallVariants)) return RSBD8G_ERR_BAD_ARG;
+    const SegSmallShape sh = seg_small_shape(int(r.key_bytes), int(variant));
+    const uint32_t cap = uint32_t(sh.threads * sh.items);
+    const uint32_t cutoff = (t && t->small_cutoff) ? t->small_cutoff : cap;
+    if (cutoff > cap) return RSBD8G_ERR_BAD_ARG;
+    const SweepGeometry g = sweep_geometry(int(r.key_bytes), false);
+    L->tile = uint32_t(g.threads * g.items);
+    L->cutoff = cutoff;
+    L->small_variant = variant;
+    L->nlarge_max = std::max<uint64_t>(1, std::min<uint64_t>(nsegs, total / (uint64_t(cutoff) + 1)));
+    L->tiles_max = total / L->tile + L->nlarge_max + 1;
+    if (L->tiles_max >= (uint64_t(1) << 32) || nsegs >= (uint64_t(1) << 32)) return RSBD8G_ERR_TOO_LARGE;
+    const uint64_t P = r.key_bytes;
+    L->ctrl = 0;
+    L->seg_hist = up(sizeof(SegControl));
+    L->zero_bytes = L->seg_hist + up(L->nlarge_max * P * kBuckets * 4);
+    L->large_seg = L->zero_bytes;
+    L->large_tbase = L->large_seg + up(L->nlarge_max * 4);
+    L->small_seg = L->large_tbase + up((L->nlarge_max + 1) * 4);
+    L->seg_mask = L->small_seg + up(nsegs * 4);
+    L->status = L->seg_mask + up(L->nlarge_max * 4);
+    L->status_bytes = up(L->tiles_max * kBuckets * 4);
+    L->total = L->status + L->status_bytes;
+    return RSBD8G_OK;
+}
+
+}  // namespace
+}  // namespace rsbd8g
+
+using namespace rsbd8g;
+
+extern "C" {
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                        const rsbd8g_segtuning *tuning, size_t *bytes) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (r.indirect != RSBD8G_DIRECT || !bytes) return RSBD8G_ERR_BAD_ARG;
+    SegLayout L;
+    if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
+    *bytes = L.total;
+    return RSBD8G_OK;
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                   const uint64_t *offsets, void *scratch, size_t scratch_bytes,
+                                                   const void *input, void *output, void *buffer,
+                                                   const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (r.indirect != RSBD8G_DIRECT) return RSBD8G_ERR_BAD_ARG;
+    if (nsegs == 0 || total == 0) return RSBD8G_OK;
+    if (!offsets || !scratch || !input || !output || !buffer) return RSBD8G_ERR_BAD_ARG;
+    if (input == output || input == buffer || output == buffer) return RSBD8G_ERR_BAD_ARG;
+    if ((reinterpret_cast<uintptr_t>(scratch) & (kA - 1)) != 0) return RSBD8G_ERR_BAD_ARG;
+    SegLayout L;
+    if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
+    if (scratch_bytes < L.total) return RSBD8G_ERR_BAD_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned char *sc = static_cast<unsigned char *>(scratch);
+    cudaError_t e;
+    {
+        LaunchTimer t(s, RSBD8G_KERNEL_MEMSET, r.key_bytes, 0, total);
+        e = cudaMemsetAsync(sc, 0, L.zero_bytes, s);
+    }
+    if (e != cudaSuccess) return RSBD8G_ERR_CUDA;
+    // the spin limit lives in the control block, written by a tiny copy (no host synchronisation)
+    const uint64_t limit = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 200000000ull : 1000000000ull;
+    if (cudaMemcpyAsync(sc + offsetof(SegControl, spin_limit_ns), &limit, sizeof limit, cudaMemcpyHostToDevice, s) !=
+        cudaSuccess)
+        return RSBD8G_ERR_CUDA;
+    SegArgs a{};
+    a.offsets = offsets;
+    a.total = total;
+    a.nsegs = uint32_t(nsegs);
+    a.cutoff = L.cutoff;
+    a.tile = L.tile;
+    a.rev = r.rev;
+    a.dmask = r.f.desc ? 0xFFu : 0u;
+    a.nlarge_max = uint32_t(L.nlarge_max);
+    a.ctrl = reinterpret_cast<SegControl *>(sc + L.ctrl);
+    a.large_seg = reinterpret_cast<uint32_t *>(sc + L.large_seg);
+    a.large_tbase = reinterpret_cast<uint32_t *>(sc + L.large_tbase);
+    a.small_seg = reinterpret_cast<uint32_t *>(sc + L.small_seg);
+    a.seg_hist = reinterpret_cast<uint32_t *>(sc + L.seg_hist);
+    a.seg_mask = reinterpret_cast<uint32_t *>(sc + L.seg_mask);
+    switch (r.key_bytes) {
+        case 1: e = launch_segmented_k1(r, a, L, sc, input, output, buffer, s); break;
+        case 2: e = launch_segmented_k2(r, a, L, sc, input, output, buffer, s); break;
+        case 4: e = launch_segmented_k4(r, a, L, sc, input, output, buffer, s); break;
+        default: e = launch_segmented_k8(r, a, L, sc, input, output, buffer, s); break;
+    }
+    return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+"""Batched (segmented) sort on the GPU: every segment bit-exact against the oracle sorting that
+segment alone, for segment lists with empty, single, small, cutoff-boundary and multi-tile
+segments, all modes that matter and all directions; graph capture and replay; and the
+per-array loop giving the same bytes."""
+import numpy as np
+import pytest
+
+from conftest import from_dev, same_bits, to_dev
+from oracle import oracle as O
+from radixsortbidi8_gb300 import synth as S
+
+pytestmark = pytest.mark.gpu
+DIRS = ["ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"]
+
+
+def _segments(lens, dt, seed):
+    lens = np.asarray(lens, dtype=np.int64)
+    offs = np.zeros(lens.size + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    n = int(offs[-1])
+    dt = np.dtype(dt)
+    a = S.float_specials(seed, n, dt) if dt.kind == "f" else S.uniform_bits(seed, n, dt)
+    if n > 10:
+        a[::9] = a[4]
+    return a, offs
+
+
+def _check(a, offs, dt, mode, direction, tuning=None):
+    import torch
+    from radixsortbidi8_gb300 import batched as B
+    inp = to_dev(a)
+    off_t = torch.from_numpy(offs).cuda()
+    s = B.SegmentedSorter(inp, off_t, direction, mode, key_dtype=dt, tuning=tuning)
+    with torch.cuda.stream(s.stream):
+        s.run()
+    assert s.status() == 0
+    got = from_dev(s.output, dt)
+    for i in range(offs.size - 1):
+        seg = a[offs[i]:offs[i + 1]]
+        assert same_bits(got[offs[i]:offs[i + 1]], O.sortcopy(seg, mode, direction)), (i, offs[i + 1] - offs[i])
+    return s
+
+
+def _lens_mixed(cutoff, tile):
+    return [0, 1, 2, 17, 0, cutoff - 1, cutoff, cutoff + 1, 3 * tile + 5, 1000, 7, 2 * tile, tile - 1,
+            tile + 1, 50000, 31, 32, 33]
+
+
+@pytest.mark.parametrize("dt,mode", [(np.uint32, "native"), (np.float32, "nativeabs"), (np.int64, "native"),
+                                     (np.float64, "native"), (np.uint16, "native"), (np.int32, "nativetieredabs"),
+                                     (np.uint8, "native")], ids=lambda x: str(getattr(x, "__name__", x)))
+def test_segmented_matches_oracle_per_segment(dt, mode):
+    from radixsortbidi8_gb300 import batched as B
+    kb = np.dtype(dt).itemsize
+    th, it = B.SMALL_SHAPES[kb][1]
+    cutoff = th * it
+    tile = 512 * (12 if kb == 8 else 16)
+    a, offs = _segments(_lens_mixed(cutoff, tile), dt, 7 + kb)
+    for d in DIRS:
+        _check(a, offs, dt, mode, d)
+
+
+def test_segmented_every_small_shape_and_cutoff():
+    from radixsortbidi8_gb300 import batched as B
+    lens = S.log_uniform_lengths(3, 400, 1, 20000)
+    a, offs = _segments(lens, np.float32, 11)
+    for v, (th, it) in enumerate(B.SMALL_SHAPES[4]):
+        for cutoff in (0, th * it // 3):
+            _check(a, offs, np.float32, "native", "dscrevorder", B.SegTuning(v, cutoff))
+
+
+def test_segmented_pass_skip_and_all_equal_segments():
+    lens = [5000, 40000, 3, 70000]
+    a = np.concatenate([np.full(5000, 7, np.uint32), S.low_bits_u32(2, 40000), np.array([1, 1, 1], np.uint32),
+                        np.full(70000, 123456, np.uint32)])
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    for d in DIRS:
+        _check(a, offs, np.uint32, "native", d)
+    f = np.where(np.arange(70000) % 3 == 0, np.float32(-0.0), np.float32(0.0))   # all keys tie
+    offs2 = np.array([0, 20000, 70000], np.int64)
+    for d in DIRS:
+        _check(f, offs2, np.float32, "native", d)
+
+
+def test_segmented_graph_replay_and_loop_agree():
+    import torch
+    from radixsortbidi8_gb300 import batched as B
+    lens = S.log_uniform_lengths(5, 2000, 16, 1 << 16)
+    a, offs = _segments(lens, np.uint32, 21)
+    inp = to_dev(a)
+    off_t = torch.from_numpy(offs).cuda()
+    s = B.SegmentedSorter(inp, off_t, key_dtype=np.uint32).capture()
+    s.output.zero_()
+    s.replay()
+    torch.cuda.synchronize()
+    assert s.status() == 0
+    got = from_dev(s.output, np.uint32)
+    loop_out = torch.empty_like(inp)
+    B.sort_each(inp, loop_out, offs, key_dtype=np.uint32)
+    torch.cuda.synchronize()
+    assert same_bits(got, from_dev(loop_out, np.uint32))
+    want = np.concatenate([np.sort(a[offs[i]:offs[i + 1]], kind="stable") for i in range(offs.size - 1)])
+    assert same_bits(got, want)
+    # new data in the same buffers, same graph
+    b = S.uniform_bits(22, a.size, np.uint32)
+    inp.copy_(to_dev(b))
+    s.replay()
+    torch.cuda.synchronize()
+    want = np.concatenate([np.sort(b[offs[i]:offs[i + 1]], kind="stable") for i in range(offs.size - 1)])
+    assert same_bits(from_dev(s.output, np.uint32), want)
+
+
+def test_segmented_lookback_timeout_reported():
+    import torch
+    from radixsortbidi8_gb300 import batched as B
+    a, offs = _segments([200000, 300000], np.uint32, 3)
+    inp = to_dev(a)
+    out, buf = torch.empty_like(inp), torch.empty_like(inp)
+    off_t = torch.from_numpy(offs).cuda()
+    scratch = torch.empty(B.segmented_scratch_bytes(np.uint32, a.size, 2), dtype=torch.uint8, device="cuda")
+    B.segmented_sortcopy(inp, out, buf, off_t, scratch, key_dtype=np.uint32, flags=1)
+    from radixsortbidi8_gb300 import api
+    assert api.scratch_status(scratch) == api.ERR_TIMEOUT
+    _check(a, offs, np.uint32, "native", "ascfwdorder")
