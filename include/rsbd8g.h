@@ -182,6 +182,53 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size
                                                    const void *input, void *output, void *buffer,
                                                    const rsbd8g_segtuning *tuning, rsbd8g_stream stream);
 
+/* The same for segments that live in separate device arrays: segment s is input_ptrs[s] ->
+ * output_ptrs[s], using buffer_ptrs[s] (each a device pointer, stored in device arrays of nsegs
+ * uint64 values); offsets (nsegs + 1 prefix sums of the lengths) only give the lengths.
+ * The serving loop launches its coalesced batches through this form. */
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                        const uint64_t *offsets, const uint64_t *input_ptrs,
+                                                        const uint64_t *output_ptrs, const uint64_t *buffer_ptrs,
+                                                        void *scratch, size_t scratch_bytes,
+                                                        const rsbd8g_segtuning *tuning, rsbd8g_stream stream);
+
+/* ---- serving loop -------------------------------------------------------------------------
+ * Continuous batching of sort requests on the current device.  rsbd8g_server_create allocates
+ * the whole device-memory budget once (buffers, scratch and tables of in-flight batches come out
+ * of it) and starts a dispatcher thread.  rsbd8g_server_submit queues one request (device input
+ * and output arrays of `count` keys, direct keys only, < 2^30 keys) from any host thread and
+ * returns at once; the dispatcher admits pending requests in arrival order while the budget and
+ * the `max_inflight` batch slots allow, coalesces the admitted requests that share a descriptor
+ * into one batched launch on its own stream, and retires batches as they finish, so requests
+ * arriving while others run are admitted and overlap on the device.  A request that can never
+ * fit the budget is refused (RSBD8G_ERR_BUSY).  Times are seconds on a steady host clock.
+ * No counterpart in the reference. */
+typedef struct rsbd8g_server rsbd8g_server;
+
+typedef struct rsbd8g_request_info {
+    rsbd8g_status status;
+    uint32_t reserved;
+    uint64_t count;
+    double submit_s, start_s, done_s;   /* submitted, launched in a batch, batch finished on the device */
+} rsbd8g_request_info;
+
+typedef struct rsbd8g_server_counters {
+    uint64_t submitted, completed, keys_completed, batches, max_coalesced, max_inflight_batches, pending;
+    uint64_t arena_used, budget;
+} rsbd8g_server_counters;
+
+RSBD8G_API rsbd8g_status rsbd8g_server_create(size_t budget_bytes, uint32_t max_inflight, rsbd8g_server **server);
+RSBD8G_API rsbd8g_status rsbd8g_server_submit(rsbd8g_server *server, const rsbd8g_desc *desc, size_t count,
+                                              const void *input, void *output, uint64_t *request_id);
+/* wait up to timeout_s for one request; returns its status (RSBD8G_ERR_TIMEOUT if still running) */
+RSBD8G_API rsbd8g_status rsbd8g_server_wait(rsbd8g_server *server, uint64_t request_id, double timeout_s,
+                                            rsbd8g_request_info *info);
+/* wait until nothing is pending or in flight */
+RSBD8G_API rsbd8g_status rsbd8g_server_drain(rsbd8g_server *server, double timeout_s);
+RSBD8G_API rsbd8g_status rsbd8g_server_stats(rsbd8g_server *server, rsbd8g_server_counters *stats);
+/* finish the batches in flight, stop the dispatcher, free the budget */
+RSBD8G_API rsbd8g_status rsbd8g_server_destroy(rsbd8g_server *server);
+
 /* Wait for the stream, then read and clear the device-side status word of a
  * scratch area used by a noalloc or segmented call (RSBD8G_OK, RSBD8G_ERR_TIMEOUT, ...). */
 RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stream);

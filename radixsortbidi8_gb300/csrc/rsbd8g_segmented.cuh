@@ -25,8 +25,7 @@ struct SegControl {
     uint32_t ntiles;          // tiles of all large segments
     uint32_t small_counter;
     uint32_t tile_counter[kMaxPasses];
-    uint64_t spin_limit_ns;
-    uint32_t pad[4];
+    uint32_t pad[6];
 };
 
 struct SegArgs {
@@ -44,9 +43,21 @@ struct SegArgs {
     uint32_t *small_seg;      // [nsegs]
     uint32_t *seg_hist;       // [nlarge_max][P][256]: counts, then bucket starts
     uint32_t *seg_mask;       // [nlarge_max]: surviving digits
+    // pointer-table form: segment s lives at ptr_in[s] / ptr_out[s] / ptr_buf[s] (separate arrays;
+    // offsets then only give the lengths); null: segment s is at offsets[s] of in / out / buf
+    const uint64_t *ptr_in;
+    const uint64_t *ptr_out;
+    const uint64_t *ptr_buf;
+    uint64_t spin_limit_ns;   // bound of every look-back wait
 };
 
 __device__ __forceinline__ uint64_t seg_len(const uint64_t *off, uint32_t s) { return off[s + 1] - off[s]; }
+
+// where segment `seg` starts in one of the three arrays
+template <typename U>
+__device__ __forceinline__ U *seg_ptr(const SegArgs &a, const uint64_t *table, const U *base, uint32_t seg) {
+    return table ? reinterpret_cast<U *>(table[seg]) : const_cast<U *>(base) + a.offsets[seg];
+}
 
 // one CTA of 1024 threads classifies every segment; a single 64-bit atomic per warp hands out
 // (list index, tile base) pairs so tile bases grow with the list index
@@ -149,7 +160,8 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
     for (uint32_t gt = t0; gt < t1;) {
         while (a.large_tbase[idx + 1] <= gt) ++idx;
         const uint32_t seg = a.large_seg[idx];
-        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
+        const uint64_t len = seg_len(a.offsets, seg);
+        const U *src = seg_ptr(a, a.ptr_in, in, seg);
         const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
         const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
@@ -157,7 +169,7 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         for (uint64_t b = k0 + (threadIdx.x & ~31u); b < k1; b += THREADS) {
             const uint64_t i = b + lane;
             const bool ok = i < k1;
-            count_key(sh, filter_key<MODE>(ok ? in[s0 + i] : U(0)), ok, a.dmask);
+            count_key(sh, filter_key<MODE>(ok ? src[i] : U(0)), ok, a.dmask);
         }
         __syncthreads();
         uint32_t *gh = a.seg_hist + size_t(idx) * P * kBuckets;
@@ -216,7 +228,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
     SegControl *c = a.ctrl;
     if (c->abort) return;
     const uint32_t T = c->ntiles, nl = c->nlarge;
-    const uint64_t spin_limit = c->spin_limit_ns;
+    const uint64_t spin_limit = a.spin_limit_ns;
     sweep_init_smem<U, MODE, false, THREADS, ITEMS, uint32_t>(smem);
     for (;;) {
         if (threadIdx.x == 0) {
@@ -233,15 +245,17 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
             continue;
         }
         const uint32_t seg = a.large_seg[idx];
-        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
+        const uint64_t len = seg_len(a.offsets, seg);
         const int k = __popc(mask), i = __popc(mask & ((1u << pass) - 1u)) + 1;
-        const U *src = (i == 1) ? in : (((k - (i - 1)) % 2 == 0) ? out : buf);
-        U *dst = ((k - i) % 2 == 0) ? out : buf;
+        U *sin = seg_ptr(a, a.ptr_in, in, seg), *sout = seg_ptr(a, a.ptr_out, out, seg);
+        U *sbuf = seg_ptr(a, a.ptr_buf, buf, seg);
+        const U *src = (i == 1) ? sin : (((k - (i - 1)) % 2 == 0) ? sout : sbuf);
+        U *dst = ((k - i) % 2 == 0) ? sout : sbuf;
         const uint32_t *bs = a.seg_hist + (size_t(idx) * passes + pass) * kBuckets;
         for (int j = threadIdx.x; j < kBuckets; j += THREADS) bstart[j] = bs[j];
         SweepTile<U, uint32_t> t;
-        t.src_k = src + s0;
-        t.dst_k = dst + s0;
+        t.src_k = src;
+        t.dst_k = dst;
         t.src_v = nullptr;
         t.dst_v = nullptr;
         t.status = status + size_t(a.large_tbase[idx]) * kBuckets;
@@ -265,8 +279,10 @@ __global__ void __launch_bounds__(256) k_seg_copy(SegArgs a, const U *__restrict
     for (uint32_t idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < nl; idx += (gridDim.x * blockDim.x) >> 5) {
         if (a.seg_mask[idx]) continue;
         const uint32_t seg = a.large_seg[idx];
-        const uint64_t s0 = a.offsets[seg], len = a.offsets[seg + 1] - s0;
-        for (uint64_t i = lane; i < len; i += 32) out[s0 + i] = in[s0 + (a.rev ? len - 1 - i : i)];
+        const uint64_t len = seg_len(a.offsets, seg);
+        const U *src = seg_ptr(a, a.ptr_in, in, seg);
+        U *dst = seg_ptr(a, a.ptr_out, out, seg);
+        for (uint64_t i = lane; i < len; i += 32) dst[i] = src[a.rev ? len - 1 - i : i];
     }
 }
 
@@ -313,9 +329,10 @@ __global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__res
         const uint32_t job = misc[0];
         if (job >= ns) break;
         const uint32_t seg = a.small_seg[job];
-        const uint64_t s0 = a.offsets[seg];
-        const uint32_t len = uint32_t(a.offsets[seg + 1] - s0);
-        for (uint32_t i = tid; i < len; i += THREADS) A[i] = in[s0 + (a.rev ? len - 1u - i : i)];
+        const uint32_t len = uint32_t(seg_len(a.offsets, seg));
+        const U *sin = seg_ptr(a, a.ptr_in, in, seg);
+        U *sout = seg_ptr(a, a.ptr_out, out, seg);
+        for (uint32_t i = tid; i < len; i += THREADS) A[i] = sin[a.rev ? len - 1u - i : i];
         // warp w ranks slots [w * chunk, min((w + 1) * chunk, len)) in steps of 32
         const uint32_t chunk = ((len + WARPS - 1) / WARPS + 31u) & ~31u;
         const uint32_t w0 = min(len, uint32_t(warp) * chunk), w1 = min(len, w0 + chunk);
@@ -380,7 +397,7 @@ __global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__res
             }
             __syncthreads();
         }
-        for (uint32_t i = tid; i < len; i += THREADS) out[s0 + i] = src[i];
+        for (uint32_t i = tid; i < len; i += THREADS) sout[i] = src[i];
         __syncthreads();
     }
 }

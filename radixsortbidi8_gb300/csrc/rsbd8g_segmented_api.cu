@@ -62,17 +62,22 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc,
     return RSBD8G_OK;
 }
 
-RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size_t total, size_t nsegs,
-                                                   const uint64_t *offsets, void *scratch, size_t scratch_bytes,
-                                                   const void *input, void *output, void *buffer,
-                                                   const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
+static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, size_t nsegs, const uint64_t *offsets,
+                                      void *scratch, size_t scratch_bytes, const void *input, void *output,
+                                      void *buffer, const uint64_t *in_ptrs, const uint64_t *out_ptrs,
+                                      const uint64_t *buf_ptrs, const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
     if (r.indirect != RSBD8G_DIRECT) return RSBD8G_ERR_BAD_ARG;
     if (nsegs == 0 || total == 0) return RSBD8G_OK;
-    if (!offsets || !scratch || !input || !output || !buffer) return RSBD8G_ERR_BAD_ARG;
-    if (input == output || input == buffer || output == buffer) return RSBD8G_ERR_BAD_ARG;
+    if (!offsets || !scratch) return RSBD8G_ERR_BAD_ARG;
+    if (!in_ptrs) {
+        if (!input || !output || !buffer) return RSBD8G_ERR_BAD_ARG;
+        if (input == output || input == buffer || output == buffer) return RSBD8G_ERR_BAD_ARG;
+    } else if (!out_ptrs || !buf_ptrs) {
+        return RSBD8G_ERR_BAD_ARG;
+    }
     if ((reinterpret_cast<uintptr_t>(scratch) & (kA - 1)) != 0) return RSBD8G_ERR_BAD_ARG;
     SegLayout L;
     if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
@@ -85,11 +90,6 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size
         e = cudaMemsetAsync(sc, 0, L.zero_bytes, s);
     }
     if (e != cudaSuccess) return RSBD8G_ERR_CUDA;
-    // the spin limit lives in the control block, written by a tiny copy (no host synchronisation)
-    const uint64_t limit = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 200000000ull : 1000000000ull;
-    if (cudaMemcpyAsync(sc + offsetof(SegControl, spin_limit_ns), &limit, sizeof limit, cudaMemcpyHostToDevice, s) !=
-        cudaSuccess)
-        return RSBD8G_ERR_CUDA;
     SegArgs a{};
     a.offsets = offsets;
     a.total = total;
@@ -105,6 +105,10 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size
     a.small_seg = reinterpret_cast<uint32_t *>(sc + L.small_seg);
     a.seg_hist = reinterpret_cast<uint32_t *>(sc + L.seg_hist);
     a.seg_mask = reinterpret_cast<uint32_t *>(sc + L.seg_mask);
+    a.ptr_in = in_ptrs;
+    a.ptr_out = out_ptrs;
+    a.ptr_buf = buf_ptrs;
+    a.spin_limit_ns = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 200000000ull : 1000000000ull;
     switch (r.key_bytes) {
         case 1: e = launch_segmented_k1(r, a, L, sc, input, output, buffer, s); break;
         case 2: e = launch_segmented_k2(r, a, L, sc, input, output, buffer, s); break;
@@ -112,6 +116,23 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size
         default: e = launch_segmented_k8(r, a, L, sc, input, output, buffer, s); break;
     }
     return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                   const uint64_t *offsets, void *scratch, size_t scratch_bytes,
+                                                   const void *input, void *output, void *buffer,
+                                                   const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
+    return segmented_common(desc, total, nsegs, offsets, scratch, scratch_bytes, input, output, buffer, nullptr,
+                            nullptr, nullptr, tuning, stream);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                        const uint64_t *offsets, const uint64_t *input_ptrs,
+                                                        const uint64_t *output_ptrs, const uint64_t *buffer_ptrs,
+                                                        void *scratch, size_t scratch_bytes,
+                                                        const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
+    return segmented_common(desc, total, nsegs, offsets, scratch, scratch_bytes, nullptr, nullptr, nullptr,
+                            input_ptrs, output_ptrs, buffer_ptrs, tuning, stream);
 }
 
 }  // extern "C"

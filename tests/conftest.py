@@ -12,6 +12,7 @@ if ROOT not in sys.path:
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: long-running case")
+    config.addinivalue_line("markers", "timeout(seconds): per-test time limit (pytest-timeout)")
 
 
 def has_gpu() -> bool:
