@@ -2,10 +2,12 @@
 compiled from Radixsortbidi8.hpp by `make -C oracle ref`) on seeded inputs.
 
 Run where the reference tree exists:   python tests/golden/make_golden.py
-Each case runs twice, each time in a fresh subprocess, because the reference snapshot
+Each case runs three times, each time in a fresh subprocess, because the reference snapshot
 has multithreading races: at some sizes it crashes or returns different orders from
 run to run.  A case is recorded as
-  "ok"        both runs agree (the sha256 of the output bytes is stored),
+  "ok"        three runs agree and the output is a permutation of the input (a check that
+              needs no sorting semantics; the sha256 of the output bytes is stored),
+  "corrupt"   a run returned something that is not a permutation of the input,
   "crash"     a run died (signal / non-zero exit),
   "unstable"  the runs disagree,
   "hang"      a run did not finish within 60 s (the reference spins forever at some sizes).
@@ -102,11 +104,17 @@ def run_case(c: dict) -> bytes:
         base = np.uint64(buf.ctypes.data)
         ptrs = base + np.arange(n, dtype=np.uint64) * np.uint64(24)
         out = O.ref_indirect(ptrs, c["dtype"], c["mode"], c["direction"], member=c["form"] == "member")
-        return ((out - base) // np.uint64(24)).astype(np.uint64).tobytes()
+        idx = ((out - base) // np.uint64(24)).astype(np.uint64)
+        perm = np.array_equal(np.sort(idx), np.arange(n, dtype=np.uint64))
+        return idx.tobytes(), perm
     a = make_input(c["gen"], c["dtype"], c["n"], c["seed"])
     if c["form"] == "inplace":
-        return O.ref_inplace(a, c["mode"], c["direction"]).tobytes()
-    return O.ref_sortcopy(a, c["mode"], c["direction"]).tobytes()
+        out = O.ref_inplace(a, c["mode"], c["direction"])
+    else:
+        out = O.ref_sortcopy(a, c["mode"], c["direction"])
+    ut = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize]
+    perm = np.array_equal(np.sort(out.view(ut)), np.sort(a.view(ut)))
+    return out.tobytes(), perm
 
 
 def _spawn(c: dict) -> tuple[str, str | None, str | None]:
@@ -118,7 +126,9 @@ def _spawn(c: dict) -> tuple[str, str | None, str | None]:
     if r.returncode != 0:
         return "crash", None, None
     line = r.stdout.strip().splitlines()[-1]
-    sha, small = line.split(" ", 1)
+    sha, perm, small = line.split(" ", 2)
+    if perm != "1":
+        return "corrupt", None, None
     return "ok", sha, (small if small != "-" else None)
 
 
@@ -130,19 +140,17 @@ def main() -> None:
     cs = cases()
 
     def both(c):
-        r1 = _spawn(c)
-        if r1[0] == "hang":
-            return dict(c, status="hang")
-        r2 = _spawn(c)
-        if r2[0] == "hang":
-            return dict(c, status="hang")
-        if r1[0] == "crash" or r2[0] == "crash":
-            return dict(c, status="crash")
-        if r1[1] != r2[1]:
+        runs = []
+        for _ in range(3):
+            r = _spawn(c)
+            if r[0] != "ok":
+                return dict(c, status=r[0])
+            runs.append(r)
+        if len({r[1] for r in runs}) != 1:
             return dict(c, status="unstable")
-        d = dict(c, status="ok", sha256=r1[1])
-        if r1[2]:
-            d["output_hex"] = r1[2]
+        d = dict(c, status="ok", sha256=runs[0][1])
+        if runs[0][2]:
+            d["output_hex"] = runs[0][2]
         return d
 
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
@@ -160,7 +168,7 @@ def main() -> None:
 
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[1] == "--case":
-        b = run_case(json.loads(sys.argv[2]))
-        print(hashlib.sha256(b).hexdigest(), b.hex() if len(b) <= 64 * 8 else "-")
+        b, perm = run_case(json.loads(sys.argv[2]))
+        print(hashlib.sha256(b).hexdigest(), int(bool(perm)), b.hex() if len(b) <= 64 * 8 else "-")
     else:
         main()

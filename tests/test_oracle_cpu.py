@@ -160,11 +160,16 @@ def test_oracle_matches_reference_golden(case):
     assert hashlib.sha256(_oracle_case_bytes(case)).hexdigest() == case["sha256"]
 
 
-def test_golden_fixture_present_and_mostly_sound():
+def test_golden_fixture_present_and_pins_every_key_type():
     cs = _golden_cases()
     assert len(cs) > 100
-    ok = sum(c["status"] == "ok" for c in cs)
-    assert ok >= 0.8 * len(cs)
+    ok = [c for c in cs if c["status"] == "ok"]
+    # the reference's multithreaded paths crash, hang or corrupt some cases (recorded as such);
+    # what is left must still pin every key type and every direction
+    assert len(ok) >= 100
+    assert {c["dtype"] for c in ok} >= {"uint8", "int8", "uint16", "int16", "uint32", "int32", "float32",
+                                         "uint64", "int64", "float64"}
+    assert {c["direction"] for c in ok} == {"ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"}
 
 
 # ---- the reference itself, live (only where it was compiled here) ---------------------------
