@@ -55,6 +55,12 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind"],
                    help="profiling aid: sort only this one array --steps times and print its timings")
+    p.add_argument("--config", default="sweep", choices=["sweep", "batched", "serving"],
+                   help="sweep: the default line; batched: segmented batches vs a per-array loop; "
+                        "serving: Poisson request stream through the serving loop")
+    p.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
+    p.add_argument("--rate", type=float, default=2000.0, help="serving: requests per second")
+    p.add_argument("--batch-scale", type=float, default=1.0, help="batched: fraction of the segment counts")
     return p.parse_args()
 
 
@@ -479,10 +485,201 @@ def single_case(args) -> dict:
             "kernels": {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 4)} for k, v in agg.items()}}
 
 
+def batched_config(args) -> dict:
+    """Batch A: 100,000 uint32 arrays, lengths log-uniform [16, 2^20] (seed 0x5EED0005), also truncated
+    at a cumulative 2^28 keys; batch B: 20,000 float64 arrays, log-uniform [64, 2^18] (seed 0x5EED0006).
+    Each batch: one captured CUDA graph per batch (segmented sort), replayed --steps times, against a
+    per-array loop of plain noalloc sorts on the same GPU; outputs compared byte for byte."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import batched as B, synth as S
+    dev = torch.device("cuda", 0)
+    res = {}
+
+    def one(name, key_bytes, kdt, lens, seed):
+        offs = np.zeros(lens.size + 1, dtype=np.int64)
+        np.cumsum(lens, out=offs[1:])
+        total = int(offs[-1])
+        t = {4: torch.int32, 8: torch.int64}[key_bytes]
+        keys = torch.empty(total, dtype=t, device=dev)
+        chunk = 1 << 27
+        for o in range(0, total, chunk):
+            m = min(chunk, total - o)
+            keys[o:o + m] = S.uniform_bits_torch(seed + o, m, key_bytes, device=dev) if key_bytes == 4 else \
+                S.float_specials_torch(seed + o, m, 8, device=dev)
+        off_t = torch.from_numpy(offs).to(dev)
+        sorter = B.SegmentedSorter(keys, off_t, key_dtype=kdt).capture()
+        for _ in range(max(1, args.warmup)):
+            sorter.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(sorter.stream)
+        for _ in range(args.steps):
+            sorter.replay()
+        e1.record(sorter.stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        assert sorter.status() == 0
+        loop_out = torch.empty_like(keys)
+        ls = torch.cuda.Stream(device=dev)
+        B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)      # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)
+        torch.cuda.synchronize()
+        loop_ms = (time.perf_counter() - t0) * 1e3
+        same = bool(torch.equal(loop_out, sorter.output))
+        res[name] = {"arrays": int(lens.size), "keys": total, "batched_ms": round(ms, 3),
+                     "batched_gkeys_s": round(total / (ms * 1e-3) / 1e9, 3), "loop_ms": round(loop_ms, 2),
+                     "loop_gkeys_s": round(total / (loop_ms * 1e-3) / 1e9, 3),
+                     "speedup_vs_loop": round(loop_ms / ms, 2), "identical_to_loop": same,
+                     "tuning": {"small_variant": sorter.tuning.small_variant,
+                                "small_cutoff": sorter.tuning.small_cutoff}}
+        del keys, off_t, sorter, loop_out
+        torch.cuda.empty_cache()
+
+    na = max(1, int(100000 * args.batch_scale))
+    lens_a = S.log_uniform_lengths(0x5EED0005, na, 16, 1 << 20)
+    cut = int(np.searchsorted(np.cumsum(lens_a), 1 << 28))
+    one("A_2p28", 4, np.uint32, lens_a[:max(1, cut)], 0x5EED0005)
+    one("A", 4, np.uint32, lens_a, 0x5EED0005)
+    nb = max(1, int(20000 * args.batch_scale))
+    one("B", 8, np.float64, S.log_uniform_lengths(0x5EED0006, nb, 64, 1 << 18), 0x5EED0006)
+    return {"config": "batched segmented sort (one captured CUDA graph per batch) vs per-array loop",
+            "steps": args.steps, "results": res}
+
+
+def serving_config(args) -> dict:
+    """Poisson arrivals at --rate req/s for --duration s; length log-uniform [2^10, 2^26]; key type
+    uniform over {uint16, int32, float32, float64}; direction asc/desc (forward order); absolute filter
+    with probability 0.5; 64 GB device budget.  Inputs are slices of device-resident pools (the loop
+    measures sort service, not host transfers).  Then the same requests, closed-loop: all queued at
+    once through the server vs a loop of plain allocating sorts."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import serving, synth as S, api
+    dev = torch.device("cuda", 0)
+    arr = S.poisson_arrivals(0x5EED0007, args.rate, args.duration)
+    nreq = arr.size
+    lens = S.log_uniform_lengths(0x5EED0007, nreq, 1 << 10, 1 << 26)
+    u = S.splitmix64(0x5EED0007, nreq, stream=41)
+    kinds = [(np.uint16, torch.int16), (np.int32, torch.int32), (np.float32, torch.int32), (np.float64, torch.int64)]
+    kind = (u % np.uint64(4)).astype(int)
+    desc = (S.splitmix64(0x5EED0007, nreq, stream=42) & np.uint64(1)).astype(int)
+    absf = (S.splitmix64(0x5EED0007, nreq, stream=43) & np.uint64(1)).astype(int)
+    pool_n = 1 << 27
+    pools = []
+    for kd, td in kinds:
+        kb = np.dtype(kd).itemsize
+        bits = S.float_specials_torch(7, pool_n, kb, device=dev) if kd in (np.float32, np.float64) else \
+            S.uniform_bits_torch(7, pool_n, kb, device=dev)
+        pools.append(bits.view(td) if bits.dtype != td else bits)
+    ring_n = 1 << 30
+    rings = [torch.empty(ring_n, dtype=td, device=dev) for _, td in kinds]
+    ring_pos = [0, 0, 0, 0]
+    ring_owner = [[], [], [], []]           # (start, end, request id) still possibly in flight
+    starts = (S.splitmix64(0x5EED0007, nreq, stream=44) % np.uint64(pool_n - (1 << 26))).astype(np.int64)
+    srv = serving.Server(budget_bytes=64 << 30, max_inflight=4)
+    ids, metas = [], []
+
+    def out_region(k, n):
+        p = ring_pos[k] if ring_pos[k] + n <= ring_n else 0
+        keep = []
+        for (a, b, rid) in ring_owner[k]:
+            if a < p + n and p < b:
+                srv.wait(rid)             # the region is about to be reused
+            else:
+                keep.append((a, b, rid))
+        ring_owner[k] = keep
+        ring_pos[k] = p + n
+        return p
+
+    t_begin = time.perf_counter()
+    for i in range(nreq):
+        delay = t_begin + arr[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        k = kind[i]
+        n = int(lens[i])
+        kd = kinds[k][0]
+        p = out_region(k, n)
+        inp = pools[k][starts[i]:starts[i] + n]
+        out = rings[k][p:p + n]
+        d = "dscfwdorder" if desc[i] else "ascfwdorder"
+        m = "nativeabs" if absf[i] else "native"
+        rid = srv.submit(inp, out, d, m, key_dtype=kd)
+        ring_owner[k].append((p, p + n, rid))
+        ids.append(rid)
+        metas.append((k, n, d, m, int(starts[i]), p))
+    srv.drain()
+    infos = [srv.wait(r) for r in ids]
+    st = srv.stats()
+    t_first = min(i.submit_s for i in infos)
+    t_last = max(i.done_s for i in infos)
+    keys = int(sum(i.count for i in infos))
+    lat = serving.latency_summary(infos)
+    # spot check: a few results against a standalone sort of the same request
+    ok = True
+    for j in list(range(0, nreq, max(1, nreq // 16)))[:16]:
+        k, n, d, m, s0, p = metas[j]
+        if p + n > ring_n or any(a < p + n and p < b for (a, b, r) in ring_owner[k] if r > ids[j]):
+            continue
+        alone = torch.empty(n, dtype=kinds[k][1], device=dev)
+        import radixsortbidi8_gb300 as rs
+        rs.radixsortcopy(pools[k][s0:s0 + n], alone, d, m, key_dtype=kinds[k][0])
+        ok &= bool(torch.equal(alone, rings[k][p:p + n]))
+    srv.close()
+    # closed loop: a prefix of the same requests, queued at once vs a plain allocating-sort loop
+    m_req = min(nreq, 2000)
+    outs = [torch.empty(int(lens[i]), dtype=kinds[kind[i]][1], device=dev) for i in range(m_req)]
+    srv2 = serving.Server(budget_bytes=64 << 30, max_inflight=4)
+    for i in range(min(m_req, 64)):          # warm-up of kernels and module loading
+        srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
+                    "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
+                    key_dtype=kinds[kind[i]][0])
+    srv2.drain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids2 = [srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
+                        "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
+                        key_dtype=kinds[kind[i]][0]) for i in range(m_req)]
+    srv2.drain()
+    served_s = time.perf_counter() - t0
+    st2 = srv2.stats()
+    srv2.close()
+    import radixsortbidi8_gb300 as rs
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(m_req):
+        rs.radixsortcopy(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
+                         "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
+                         key_dtype=kinds[kind[i]][0])
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    keys2 = int(lens[:m_req].sum())
+    del ids2, api
+    return {"config": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s, lengths log-uniform "
+                      f"[2^10, 2^26], {{u16, i32, f32, f64}}, asc/desc, abs p=0.5, 64 GB budget",
+            "requests": nreq, "offered_gkeys_s": round(float(lens.sum()) / args.duration / 1e9, 3),
+            "served_gkeys_s": round(keys / (t_last - t_first) / 1e9, 3), "latency": lat,
+            "batches": st["batches"], "max_coalesced": st["max_coalesced"],
+            "max_inflight_batches": st["max_inflight_batches"], "spot_checks_identical": ok,
+            "closed_loop": {"requests": m_req, "keys": keys2,
+                            "served_gkeys_s": round(keys2 / served_s / 1e9, 3),
+                            "plain_loop_gkeys_s": round(keys2 / loop_s / 1e9, 3),
+                            "speedup": round(loop_s / served_s, 2), "batches": st2["batches"]}}
+
+
 def main():
     args = parse_args()
     if args.case:
         print(json.dumps(single_case(args)), flush=True)
+        return
+    if args.config == "batched":
+        print(json.dumps(batched_config(args)), flush=True)
+        return
+    if args.config == "serving":
+        print(json.dumps(serving_config(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

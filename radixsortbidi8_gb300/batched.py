@@ -113,7 +113,9 @@ class SegmentedSorter:
         return self
 
     def replay(self):
-        self.graph.replay()
+        import torch
+        with torch.cuda.stream(self.stream):       # a graph launches on the current stream
+            self.graph.replay()
         return self.output
 
     def status(self) -> int:
