@@ -1,9 +1,11 @@
 """Seeded synthetic workloads of the benchmark configurations (deterministic, counter-based).
 
-Every value is a function of (seed, index) through splitmix64, so the same call gives
-the same data on any host; the torch variants compute the identical integer stream on
-the GPU for the large configurations (floating-point transforms such as Box-Muller may
-differ in the last bit between numpy and torch, which no test relies on).
+Every value is a function of (seed, index) through splitmix64, and the numpy generators use
+only correctly rounded basic arithmetic (no log/exp/cos from the platform's maths library), so
+the same call gives the same bits on any host -- the reference-generated fixtures depend on it.
+The torch variants compute the identical integer stream on the GPU for the large benchmark
+inputs; their floating-point shaping uses device maths functions and is not bit-identical to
+the numpy one, which nothing relies on.
 
 Workloads (the reference benchmarks random bit patterns only; these stand in for the
 configurations it is measured on):
@@ -51,9 +53,24 @@ def low_bits_u32(seed: int, n: int, bits: int = 12) -> np.ndarray:
 
 
 def normal(seed: int, n: int, stream: int = 0) -> np.ndarray:
-    u1 = unit_interval(splitmix64(seed, n, stream=2 * stream + 1))
-    u2 = unit_interval(splitmix64(seed, n, stream=2 * stream + 2))
-    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    """Approximately N(0, 1): the Irwin-Hall sum of 12 uniforms minus 6 (summed in a fixed order,
+    so every platform rounds identically)."""
+    acc = np.zeros(n, dtype=np.float64)
+    for k in range(12):
+        acc += unit_interval(splitmix64(seed, n, stream=100 * stream + k + 1))
+    return acc - 6.0
+
+
+def exp2_det(t: np.ndarray) -> np.ndarray:
+    """2**t from basic arithmetic only: ldexp of a fixed-order Taylor polynomial of 2**f, f in [0, 1)."""
+    i = np.floor(t)
+    x = (t - i) * 0.6931471805599453
+    p = np.ones_like(x)
+    term = np.ones_like(x)
+    for k in range(1, 12):
+        term = term * x / float(k)
+        p = p + term
+    return np.ldexp(p, i.astype(np.int64))
 
 
 def float_specials(seed: int, n: int, dtype=np.float32, sigma: float = 1e3) -> np.ndarray:
@@ -80,7 +97,7 @@ def records24(seed: int, n: int) -> np.ndarray:
     10% duplicate the key of an earlier random record."""
     rec = np.zeros(n, dtype=[("id", "<u8"), ("key", "<f8"), ("tag", "<u4"), ("pad", "<u4")])
     rec["id"] = np.arange(n, dtype=np.uint64)
-    key = np.exp(2.0 * normal(seed, n))
+    key = exp2_det(normal(seed, n) * (2.0 / 0.6931471805599453))      # lognormal(0, 2)
     sgn = (splitmix64(seed, n, stream=11) & np.uint64(1)).astype(bool)
     key = np.where(sgn, -key, key)
     dup = unit_interval(splitmix64(seed, n, stream=12)) <= 0.1
