@@ -173,6 +173,22 @@ def active_passes(bits, name: str) -> int:
     return cnt
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest per-step time over all ranks (every rank sorts its own replica of the workload)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gkeys(keys_per_rank_step: int, world: int, ms_step: float) -> float:
+    """Whole-job throughput: the keys all ranks sorted in one step over the slowest rank's step time."""
+    return world * keys_per_rank_step / (ms_step * 1e-3) / 1e9
+
+
 def gb300_arm(args, rank: int, world: int):
     import numpy as np
     import torch
@@ -231,14 +247,9 @@ def gb300_arm(args, rank: int, world: int):
     # correctness of the timed outputs: sorted by the filtered key, same multiset of bits
     check = verify_outputs(arrays, bufs)
 
-    ms_step = ms_total / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ms_total / args.steps, world, dev)
     keys_step = 3 * n
-    value = world * keys_step / (ms_step * 1e-3) / 1e9
+    value = whole_job_gkeys(keys_step, world, ms_step)
 
     peak, peak_kind = measured_peak()
     # per-sort and per-kernel breakdown from the launch records (launch order is fixed per step)
