@@ -16,10 +16,14 @@
 //   indirection: member object pointer, pointer member (second level), getter member
 //   function (+ arguments), type+offset (<T, offset1, ..., offset2>), and simple
 //   second-level arrays (T *const *)                      Radixsortbidi8.hpp:60590-61739
+//   index arguments and isindexed2 of the indirect forms (folded into one byte offset)
+//                                                         Radixsortbidi8.hpp:2412-2470, :2787-2813
+//   8-bit keys: the single-part noalloc forms without a buffer argument
+//                                                         Radixsortbidi8.hpp:60193-60395
 // Getters are evaluated on the host for every element (C++ member functions cannot be
 // called from the device), so their objects must be host-accessible; the keys then travel
-// to the device and the pointers are sorted there.  Indexed second-level indirection
-// (isindexed2 = true) is not available on this path.
+// to the device and the pointers are sorted there.  Getters are offered in the allocating
+// forms only: the noalloc forms could not hold the host-evaluated keys.
 #pragma once
 
 #include <cuda_runtime_api.h>
@@ -104,12 +108,14 @@ inline void setstream(rsbd8g_stream stream) noexcept { gpu_detail::stream_slot()
 
 // Scratch bytes (device) the noalloc forms need; the stand-in for the index buffer that
 // rsbd8::allocatearray sizes in the reference (Radixsortbidi8.hpp:59928).
+// For 8-bit keys it also holds the ping-pong buffer of the single-part forms.
 template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
           typename T>
 inline std::size_t gpuscratchbytes(std::size_t count) noexcept {
     rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>();
     std::size_t b = 0;
-    return rsbd8g_scratch_bytes(&d, count, &b) == RSBD8G_OK ? b : 0;
+    if (rsbd8g_scratch_bytes(&d, count, &b) != RSBD8G_OK) return 0;
+    return sizeof(T) == 1 ? ((b + 255u) & ~std::size_t(255u)) + count : b;
 }
 
 // ---- plain arrays ------------------------------------------------------------------------------
@@ -170,68 +176,224 @@ radixsortnoalloc(std::size_t count, void *pzeroedindices, T *input, T *buffer, b
     radixsortnoalloc<direction, mode, T>(count, 1u, nullptr, pzeroedindices, input, buffer, movetobuffer);
 }
 
-// ---- simple second-level arrays: T *const *input, key at byte indirection2 behind each pointer -----
-
+// single-part forms of 8-bit keys: no buffer argument, the buffer sits at the end of the scratch
 template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
-          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T>
-[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>>, bool>
-radixsortcopy(std::size_t count, T *const *input, T **output, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
-    static_cast<void>(mmapflags);
-    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, std::remove_cv_t<T>>(RSBD8G_MEMBER, indirection2);
-    return gpu_detail::ok(rsbd8g_radixsortcopy(&d, count, input, output, gpu_detail::stream_slot()));
+          typename T>
+inline std::enable_if_t<gpu_detail::iskeytype<T> && sizeof(T) == 1, void>
+radixsortcopynoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                     T const *input, T *output) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>();
+    const std::size_t all = gpuscratchbytes<direction, mode, T>(count), own = all - count;
+    rsbd8g_radixsortcopynoalloc(&d, count, pzeroedindices, own, input, output,
+                                static_cast<unsigned char *>(pzeroedindices) + own, gpu_detail::stream_slot());
 }
 
 template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
-          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T>
-[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>>, bool>
-radixsort(std::size_t count, T **input, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
-    static_cast<void>(mmapflags);
-    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, std::remove_cv_t<T>>(RSBD8G_MEMBER, indirection2);
-    return gpu_detail::ok(rsbd8g_radixsort(&d, count, input, gpu_detail::stream_slot()));
+          typename T>
+inline std::enable_if_t<gpu_detail::iskeytype<T> && sizeof(T) == 1, void>
+radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                 T *input) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>();
+    const std::size_t all = gpuscratchbytes<direction, mode, T>(count), own = all - count;
+    rsbd8g_radixsortnoalloc(&d, count, pzeroedindices, own, input,
+                            static_cast<unsigned char *>(pzeroedindices) + own, 0, gpu_detail::stream_slot());
 }
 
-// ---- member object pointer (key member, or a pointer member for second-level indirection) --------
+// ---- indirection: where the key sits --------------------------------------------------------------
+// In the member-object-pointer, type+offset and simple second-level forms the key of element i
+// lies at byte
+//     offset1 + indirection2 + (index1 + index2) * sizeof(key)
+// of the object input[i] points to: indirection2 and every index argument only move the key within
+// the object (splitgetobject Radixsortbidi8.hpp:2412-2470, indirectinput1 :2740-2770,
+// indirectinput2 :2787-2813), so they fold into one byte offset shared by all elements.
+// A data member or type+offset form whose type is itself a pointer makes the reference stop at a
+// static assertion ("third level indirection", Radixsortbidi8.hpp:2762-2764); the facade gives it
+// the natural meaning instead: the pointer at offset1 (+ index1 pointers) is loaded and the key
+// sits at indirection2 + index2 * sizeof(key) behind it.
 
-template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
-          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
-          typename V>
-[[nodiscard]] inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)>, bool>
-radixsortcopy(std::size_t count, V *const *input, V **output, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
-    static_cast<void>(mmapflags);
-    using M = typename gpu_detail::memberinfo<indirection1>::membertype;
-    const std::ptrdiff_t off = gpu_detail::memberoffset<indirection1>(indirection1);
-    if constexpr (std::is_pointer_v<M>) {
-        using T = std::remove_cv_t<std::remove_pointer_t<M>>;
-        static_assert(gpu_detail::iskeytype<T>, "unsupported key type");
-        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>(RSBD8G_MEMBER2, off, indirection2);
-        return gpu_detail::ok(rsbd8g_radixsortcopy(&d, count, input, output, gpu_detail::stream_slot()));
+namespace gpu_detail {
+
+template <typename... A>
+constexpr bool indicesok{sizeof...(A) <= 2 && (std::is_integral_v<std::remove_cv_t<std::remove_reference_t<A>>> && ...)};
+
+template <bool isindexed2, typename... A>
+constexpr void checkindices() {
+    static_assert(indicesok<A...>, "at most two integer index arguments");
+    static_assert(!isindexed2 || sizeof...(A) >= 1, "isindexed2 needs an index argument");
+    static_assert(sizeof...(A) < 2 || isindexed2, "two index arguments need isindexed2");
+}
+
+// descriptor of an indirect sort of keys of type K; pointerlevel: the object holds a pointer to
+// the key's object instead of the key
+template <sortingdirection direction, sortingmode mode, typename K, bool pointerlevel, bool isindexed2,
+          typename... A>
+inline rsbd8g_desc indirectdesc(std::ptrdiff_t offset1, std::ptrdiff_t indirection2, A... index) {
+    checkindices<isindexed2, A...>();
+    std::ptrdiff_t ix[2]{0, 0};
+    [[maybe_unused]] std::size_t k = 0;
+    ((ix[k++] = std::ptrdiff_t(index)), ...);
+    if constexpr (!pointerlevel) {
+        return makedesc<direction, mode, K>(RSBD8G_MEMBER,
+                                            offset1 + indirection2 + (ix[0] + ix[1]) * std::ptrdiff_t(sizeof(K)));
     } else {
-        static_assert(gpu_detail::iskeytype<M>, "unsupported key type");
-        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, M>(RSBD8G_MEMBER, off);
-        return gpu_detail::ok(rsbd8g_radixsortcopy(&d, count, input, output, gpu_detail::stream_slot()));
+        // one index: first level unless isindexed2; two indices: first and second level
+        const std::ptrdiff_t i1 = (sizeof...(A) == 2 || !isindexed2) ? ix[0] : 0;
+        const std::ptrdiff_t i2 = sizeof...(A) == 2 ? ix[1] : (isindexed2 ? ix[0] : 0);
+        return makedesc<direction, mode, K>(RSBD8G_MEMBER2, offset1 + i1 * std::ptrdiff_t(sizeof(void *)),
+                                            indirection2 + i2 * std::ptrdiff_t(sizeof(K)));
     }
 }
 
+inline std::size_t scratchfor(const rsbd8g_desc &d, std::size_t count) {
+    std::size_t b = 0;
+    return rsbd8g_scratch_bytes(&d, count, &b) == RSBD8G_OK ? b : 0;
+}
+
+inline bool copyindirect(const rsbd8g_desc &d, std::size_t count, const void *input, void *output) {
+    return ok(rsbd8g_radixsortcopy(&d, count, input, output, stream_slot()));
+}
+
+inline bool sortindirect(const rsbd8g_desc &d, std::size_t count, void *input) {
+    return ok(rsbd8g_radixsort(&d, count, input, stream_slot()));
+}
+
+inline void copyindirectnoalloc(const rsbd8g_desc &d, std::size_t count, void *scratch, const void *input,
+                                void *output, void *buffer) {
+    rsbd8g_radixsortcopynoalloc(&d, count, scratch, scratchfor(d, count), input, output, buffer, stream_slot());
+}
+
+inline void sortindirectnoalloc(const rsbd8g_desc &d, std::size_t count, void *scratch, void *input, void *buffer,
+                                bool movetobuffer) {
+    rsbd8g_radixsortnoalloc(&d, count, scratch, scratchfor(d, count), input, buffer, movetobuffer ? 1 : 0,
+                            stream_slot());
+}
+
+}  // namespace gpu_detail
+
+// Scratch bytes (device) of the noalloc forms with indirection, for keys of type K.
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          typename K>
+inline std::size_t gpuscratchbytesindirect(std::size_t count) noexcept {
+    return gpu_detail::scratchfor(gpu_detail::makedesc<direction, mode, K>(RSBD8G_MEMBER), count);
+}
+
+// ---- simple second-level arrays: T *const *input, the key of type T at the folded offset ---------
+
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T, typename... A>
+[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>> && gpu_detail::indicesok<A...>, bool>
+radixsortcopy(std::size_t count, T *const *input, T **output, int mmapflags = 0, A... index) noexcept {
+    static_cast<void>(mmapflags);
+    return gpu_detail::copyindirect(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<T>, false, isindexed2>(0, indirection2, index...),
+        count, input, output);
+}
+
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T, typename... A>
+[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>> && gpu_detail::indicesok<A...>, bool>
+radixsort(std::size_t count, T **input, int mmapflags = 0, A... index) noexcept {
+    static_cast<void>(mmapflags);
+    return gpu_detail::sortindirect(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<T>, false, isindexed2>(0, indirection2, index...),
+        count, input);
+}
+
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T, typename... A>
+inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>> && gpu_detail::indicesok<A...>, void>
+radixsortcopynoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                     T *const *input, T **output, T **buffer, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::copyindirectnoalloc(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<T>, false, isindexed2>(0, indirection2, index...),
+        count, pzeroedindices, input, output, buffer);
+}
+
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          std::ptrdiff_t indirection2 = 0, bool isindexed2 = false, typename T, typename... A>
+inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<T>> && gpu_detail::indicesok<A...>, void>
+radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                 T **input, T **buffer, bool movetobuffer = false, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::sortindirectnoalloc(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<T>, false, isindexed2>(0, indirection2, index...),
+        count, pzeroedindices, input, buffer, movetobuffer);
+}
+
+// ---- member object pointer: the key member (or a pointer member, see above) ---------------------
+
+namespace gpu_detail {
+
+template <auto member>
+using memberkey = std::remove_cv_t<std::remove_pointer_t<typename memberinfo<member>::membertype>>;
+
+template <auto member>
+constexpr bool memberispointer{std::is_pointer_v<typename memberinfo<member>::membertype>};
+
+template <auto indirection1, sortingdirection direction, sortingmode mode, std::ptrdiff_t indirection2,
+          bool isindexed2, typename... A>
+inline rsbd8g_desc memberdesc(A... index) {
+    static_assert(iskeytype<memberkey<indirection1>>, "unsupported key type");
+    return indirectdesc<direction, mode, memberkey<indirection1>, memberispointer<indirection1>, isindexed2>(
+        memberoffset<indirection1>(indirection1), indirection2, index...);
+}
+
+}  // namespace gpu_detail
+
 template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
           sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
-          typename V>
-[[nodiscard]] inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)>, bool>
-radixsort(std::size_t count, V **input, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
+          typename V, typename... A>
+[[nodiscard]] inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)> &&
+                                          gpu_detail::indicesok<A...>, bool>
+radixsortcopy(std::size_t count, V *const *input, V **output, int mmapflags = 0, A... index) noexcept {
     static_cast<void>(mmapflags);
-    using M = typename gpu_detail::memberinfo<indirection1>::membertype;
-    const std::ptrdiff_t off = gpu_detail::memberoffset<indirection1>(indirection1);
-    if constexpr (std::is_pointer_v<M>) {
-        using T = std::remove_cv_t<std::remove_pointer_t<M>>;
-        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>(RSBD8G_MEMBER2, off, indirection2);
-        return gpu_detail::ok(rsbd8g_radixsort(&d, count, input, gpu_detail::stream_slot()));
-    } else {
-        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, M>(RSBD8G_MEMBER, off);
-        return gpu_detail::ok(rsbd8g_radixsort(&d, count, input, gpu_detail::stream_slot()));
-    }
+    return gpu_detail::copyindirect(
+        gpu_detail::memberdesc<indirection1, direction, mode, indirection2, isindexed2>(index...), count, input,
+        output);
+}
+
+template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... A>
+[[nodiscard]] inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)> &&
+                                          gpu_detail::indicesok<A...>, bool>
+radixsort(std::size_t count, V **input, int mmapflags = 0, A... index) noexcept {
+    static_cast<void>(mmapflags);
+    return gpu_detail::sortindirect(
+        gpu_detail::memberdesc<indirection1, direction, mode, indirection2, isindexed2>(index...), count, input);
+}
+
+template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... A>
+inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)> && gpu_detail::indicesok<A...>, void>
+radixsortcopynoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                     V *const *input, V **output, V **buffer, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::copyindirectnoalloc(
+        gpu_detail::memberdesc<indirection1, direction, mode, indirection2, isindexed2>(index...), count,
+        pzeroedindices, input, output, buffer);
+}
+
+template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... A>
+inline std::enable_if_t<std::is_member_object_pointer_v<decltype(indirection1)> && gpu_detail::indicesok<A...>, void>
+radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                 V **input, V **buffer, bool movetobuffer = false, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::sortindirectnoalloc(
+        gpu_detail::memberdesc<indirection1, direction, mode, indirection2, isindexed2>(index...), count,
+        pzeroedindices, input, buffer, movetobuffer);
 }
 
 // ---- getter member function (evaluated on the host), with optional extra arguments ----------------
@@ -279,37 +441,65 @@ radixsort(std::size_t count, V **input, int mmapflags = 0, vararguments &&...var
     return good;
 }
 
-// ---- type + offset: <T, indirection1, direction, mode, indirection2> -----------------------------
-// T not a pointer: the key of type T sits at byte indirection1 of each object.
-// T a pointer type U *: each object holds a pointer at byte indirection1 and the key of type U sits
-// at byte indirection2 behind it.
+// ---- type + offset: <T, indirection1, direction, mode, indirection2, isindexed2> ------------------
+// T not a pointer: the key of type T at byte indirection1 (folded with indirection2 and the
+// indices as above).  T a pointer type U *: the pointer at byte indirection1, the key of type U
+// behind it (see above).
 
 template <typename T, std::ptrdiff_t indirection1 = 0, sortingdirection direction = sortingdirection::ascfwdorder,
           sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
-          typename V>
-[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>>, bool>
-radixsortcopy(std::size_t count, V *const *input, V **output, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
+          typename V, typename... A>
+[[nodiscard]] inline std::enable_if_t<
+    gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>> && gpu_detail::indicesok<A...>, bool>
+radixsortcopy(std::size_t count, V *const *input, V **output, int mmapflags = 0, A... index) noexcept {
     static_cast<void>(mmapflags);
-    using K = std::remove_cv_t<std::remove_pointer_t<T>>;
-    rsbd8g_desc d = std::is_pointer_v<T> ? gpu_detail::makedesc<direction, mode, K>(RSBD8G_MEMBER2, indirection1,
-                                                                                    indirection2)
-                                         : gpu_detail::makedesc<direction, mode, K>(RSBD8G_MEMBER, indirection1);
-    return gpu_detail::ok(rsbd8g_radixsortcopy(&d, count, input, output, gpu_detail::stream_slot()));
+    return gpu_detail::copyindirect(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<std::remove_pointer_t<T>>, std::is_pointer_v<T>,
+                                 isindexed2>(indirection1, indirection2, index...),
+        count, input, output);
 }
 
 template <typename T, std::ptrdiff_t indirection1 = 0, sortingdirection direction = sortingdirection::ascfwdorder,
           sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
-          typename V>
-[[nodiscard]] inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>>, bool>
-radixsort(std::size_t count, V **input, int mmapflags = 0) noexcept {
-    static_assert(!isindexed2, "indexed second-level indirection is not available on the GPU path");
+          typename V, typename... A>
+[[nodiscard]] inline std::enable_if_t<
+    gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>> && gpu_detail::indicesok<A...>, bool>
+radixsort(std::size_t count, V **input, int mmapflags = 0, A... index) noexcept {
     static_cast<void>(mmapflags);
-    using K = std::remove_cv_t<std::remove_pointer_t<T>>;
-    rsbd8g_desc d = std::is_pointer_v<T> ? gpu_detail::makedesc<direction, mode, K>(RSBD8G_MEMBER2, indirection1,
-                                                                                    indirection2)
-                                         : gpu_detail::makedesc<direction, mode, K>(RSBD8G_MEMBER, indirection1);
-    return gpu_detail::ok(rsbd8g_radixsort(&d, count, input, gpu_detail::stream_slot()));
+    return gpu_detail::sortindirect(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<std::remove_pointer_t<T>>, std::is_pointer_v<T>,
+                                 isindexed2>(indirection1, indirection2, index...),
+        count, input);
+}
+
+template <typename T, std::ptrdiff_t indirection1 = 0, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... A>
+inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>> &&
+                            gpu_detail::indicesok<A...>, void>
+radixsortcopynoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                     V *const *input, V **output, V **buffer, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::copyindirectnoalloc(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<std::remove_pointer_t<T>>, std::is_pointer_v<T>,
+                                 isindexed2>(indirection1, indirection2, index...),
+        count, pzeroedindices, input, output, buffer);
+}
+
+template <typename T, std::ptrdiff_t indirection1 = 0, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... A>
+inline std::enable_if_t<gpu_detail::iskeytype<std::remove_cv_t<std::remove_pointer_t<T>>> &&
+                            gpu_detail::indicesok<A...>, void>
+radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                 V **input, V **buffer, bool movetobuffer = false, A... index) noexcept {
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    gpu_detail::sortindirectnoalloc(
+        gpu_detail::indirectdesc<direction, mode, std::remove_cv_t<std::remove_pointer_t<T>>, std::is_pointer_v<T>,
+                                 isindexed2>(indirection1, indirection2, index...),
+        count, pzeroedindices, input, buffer, movetobuffer);
 }
 
 }  // namespace rsbd8

@@ -61,6 +61,11 @@ struct Rec24 {
     std::uint32_t pad;
 };
 
+struct Rec4 {           // the records of oracle/ref_forms.cpp: id, then 32-bit keys a b c d
+    std::uint64_t id;
+    std::uint32_t a, b, c, d;
+};
+
 static std::uint64_t splitmix(std::uint64_t &s) {
     std::uint64_t z = (s += 0x9E3779B97F4A7C15ull);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -218,10 +223,107 @@ int main(int argc, char **argv) {
         dump(outdir, "rec_member_dscfwdorder_idx.bin", idx);
         CHECK((rsbd8::radixsort<double, 8, rsbd8::sortingdirection::dscfwdorder>(n, dp)));
         auto pi = tohost(dp, n);
-        for (std::size_t i = 0; i < n; ++i) CHECK_IDX: if (std::uint64_t(pi[i] - drec) != idx[i]) { ++failures; break; }
+        for (std::size_t i = 0; i < n; ++i) if (std::uint64_t(pi[i] - drec) != idx[i]) { ++failures; break; }
         cudaFree(drec);
         cudaFree(dp);
         cudaFree(dpo);
+    }
+    {  // indexed / offset indirection forms (oracle/ref_forms.cpp runs the same calls on the reference);
+       // each order is written as "<form>: i0 ... i5" for the comparison with tests/golden/ref_forms.json
+        constexpr int n = 6;
+        const std::uint32_t av[n]{5, 3, 9, 1, 7, 2}, bv[n]{10, 60, 20, 50, 30, 40}, cv[n]{6, 5, 4, 3, 2, 1},
+            dv[n]{1, 3, 5, 2, 4, 6};
+        std::vector<Rec4> h(n);
+        for (int i = 0; i < n; ++i) h[i] = Rec4{std::uint64_t(i), av[i], bv[i], cv[i], dv[i]};
+        Rec4 *drec = todev(h);
+        std::vector<Rec4 *> hp(n);
+        std::vector<std::uint32_t *> hk(n);
+        for (int i = 0; i < n; ++i) {
+            hp[i] = drec + i;
+            hk[i] = &drec[i].a;
+        }
+        Rec4 **din = todev(hp), **dout = nullptr, **dbuf = nullptr;
+        std::uint32_t **kin = todev(hk), **kout = nullptr, **kbuf = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), n * sizeof(void *));
+        cudaMalloc(reinterpret_cast<void **>(&dbuf), n * sizeof(void *));
+        cudaMalloc(reinterpret_cast<void **>(&kout), n * sizeof(void *));
+        cudaMalloc(reinterpret_cast<void **>(&kbuf), n * sizeof(void *));
+        void *scratch = nullptr;
+        cudaMalloc(&scratch, rsbd8::gpuscratchbytesindirect<rsbd8::sortingdirection::ascfwdorder,
+                                                            rsbd8::sortingmode::native, std::uint32_t>(n));
+        std::string forms;
+        auto show = [&](const char *t, Rec4 **d) {
+            auto o = tohost(d, n);
+            forms += t;
+            forms += ":";
+            for (auto p : o) forms += " " + std::to_string(p - drec);
+            forms += "\n";
+        };
+        auto showk = [&](const char *t, std::uint32_t **d) {
+            auto o = tohost(d, n);
+            forms += t;
+            forms += ":";
+            for (auto p : o) forms += " " + std::to_string((reinterpret_cast<char *>(p) - 8 - reinterpret_cast<char *>(drec)) / 24);
+            forms += "\n";
+        };
+        constexpr auto A = rsbd8::sortingdirection::ascfwdorder;
+        constexpr auto D = rsbd8::sortingdirection::dscfwdorder;
+        constexpr auto N = rsbd8::sortingmode::native;
+        CHECK(rsbd8::radixsortcopy<&Rec4::a>(n, din, dout)); show("member a", dout);
+        CHECK((rsbd8::radixsortcopy<&Rec4::a, A, N, 4>(n, din, dout))); show("member a, indirection2 4", dout);
+        CHECK(rsbd8::radixsortcopy<&Rec4::a>(n, din, dout, 0, 1)); show("member a, index 1", dout);
+        CHECK((rsbd8::radixsortcopy<&Rec4::a, A, N, 4>(n, din, dout, 0, 1))); show("member a, indirection2 4, index 1", dout);
+        CHECK((rsbd8::radixsortcopy<&Rec4::a, A, N, 0, true>(n, din, dout, 0, 2))); show("member a, isindexed2, index 2", dout);
+        CHECK((rsbd8::radixsortcopy<&Rec4::a, A, N, 4, true>(n, din, dout, 0, 1))); show("member a, indirection2 4, isindexed2, index 1", dout);
+        // the noalloc form of the same call
+        rsbd8::radixsortcopynoalloc<&Rec4::a, A, N, 0, true>(n, 0u, nullptr, scratch, din, dout, dbuf, 1, 2);
+        show("member a, isindexed2, indices 1 2", dout);
+        CHECK(rsbd8g_scratch_status(scratch, nullptr) == RSBD8G_OK);
+        CHECK((rsbd8::radixsortcopy<&Rec4::a, D, N, 0, true>(n, din, dout, 0, 1, 2))); show("member a desc, isindexed2, indices 1 2", dout);
+        CHECK((rsbd8::radixsortcopy<std::uint32_t, 8>(n, din, dout))); show("offset 8", dout);
+        CHECK((rsbd8::radixsortcopy<std::uint32_t, 8, A, N, 4>(n, din, dout))); show("offset 8, indirection2 4", dout);
+        CHECK((rsbd8::radixsortcopy<std::uint32_t, 8>(n, din, dout, 0, 2))); show("offset 8, index 2", dout);
+        {   // in-place noalloc form, on a copy of the pointer array
+            Rec4 **dwork = todev(hp);
+            rsbd8::radixsortnoalloc<std::uint32_t, 8, A, N, 0, true>(n, 0u, nullptr, scratch, dwork, dbuf, false, 3);
+            show("offset 8, isindexed2, index 3", dwork);
+            cudaFree(dwork);
+        }
+        CHECK((rsbd8::radixsortcopy<A, N, 4>(n, kin, kout))); showk("second level, indirection2 4", kout);
+        rsbd8::radixsortcopynoalloc<A, N, 0, true>(n, 0u, nullptr, scratch, kin, kout, kbuf, 2);
+        showk("second level, isindexed2, index 2", kout);
+        CHECK((rsbd8::radixsortcopy<A, N, 4, true>(n, kin, kout, 0, 1))); showk("second level, indirection2 4, isindexed2, index 1", kout);
+        CHECK(rsbd8g_scratch_status(scratch, nullptr) == RSBD8G_OK);
+        std::fputs(forms.c_str(), stdout);
+        if (!outdir.empty()) {
+            FILE *f = std::fopen((outdir + "/forms.txt").c_str(), "w");
+            std::fputs(forms.c_str(), f);
+            std::fclose(f);
+        }
+        cudaFree(drec);
+        cudaFree(din);
+        cudaFree(dout);
+        cudaFree(dbuf);
+        cudaFree(kin);
+        cudaFree(kout);
+        cudaFree(kbuf);
+        cudaFree(scratch);
+    }
+    {  // 8-bit keys: the single-part noalloc forms (no buffer argument)
+        std::vector<std::int8_t> h{5, -3, 9, -128, 127, 0, -3, 5};
+        std::int8_t *din = todev(h), *dout = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), h.size());
+        void *scratch = nullptr;
+        cudaMalloc(&scratch, rsbd8::gpuscratchbytes<rsbd8::sortingdirection::ascfwdorder, rsbd8::sortingmode::native,
+                                                    std::int8_t>(h.size()));
+        rsbd8::radixsortcopynoalloc(h.size(), 0u, nullptr, scratch, din, dout);
+        CHECK((tohost(dout, h.size()) == std::vector<std::int8_t>{-128, -3, -3, 0, 5, 5, 9, 127}));
+        rsbd8::radixsortnoalloc<rsbd8::sortingdirection::dscfwdorder>(h.size(), 0u, nullptr, scratch, din);
+        CHECK((tohost(din, h.size()) == std::vector<std::int8_t>{127, 9, 5, 5, 0, -3, -3, -128}));
+        CHECK(rsbd8g_scratch_status(scratch, nullptr) == RSBD8G_OK);
+        cudaFree(din);
+        cudaFree(dout);
+        cudaFree(scratch);
     }
     std::printf("%s (%d failures)\n", failures ? "FAIL" : "PASS", failures);
     return failures ? 1 : 0;

@@ -1,7 +1,9 @@
 """The C++ facade include/rsbd8.hpp: it compiles with the reference's call forms (CPU), and the
 facade program runs the reference's known-answer cases on the GPU and writes random cases
 that are compared with the oracle here."""
+import json
 import os
+import sys
 import shutil
 import subprocess
 
@@ -50,3 +52,24 @@ def test_facade_program_on_gpu(tmp_path):
     keys = np.fromfile(out / "rec_keys.bin", dtype=np.float64)
     idx = np.fromfile(out / "rec_member_dscfwdorder_idx.bin", dtype=np.uint64)
     assert np.array_equal(idx.astype(np.int64), O.numpy_sort_indices(keys, "native", "dscfwdorder"))
+    # the indexed / offset indirection forms give the reference's own orders
+    with open(os.path.join(ROOT, "tests", "golden", "ref_forms.json")) as f:
+        want = json.load(f)["forms"]
+    got = {}
+    for line in (out / "forms.txt").read_text().splitlines():
+        name, _, rest = line.partition(":")
+        got[name] = [int(x) for x in rest.split()]
+    assert got == want
+
+
+def test_ref_forms_fixture_matches_reference_binary():
+    """tests/golden/ref_forms.json is what the reference itself prints (where it was built here)."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_forms")
+    if not os.path.exists(exe):
+        pytest.skip("oracle/_ref/ref_forms not built (the reference tree is absent)")
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from make_ref_forms import parse
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    with open(os.path.join(ROOT, "tests", "golden", "ref_forms.json")) as f:
+        assert parse(out) == json.load(f)["forms"]
+    assert "all calls returned true: 1" in out
