@@ -352,23 +352,24 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
         dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
     }
     // warp multisplit in slot order: the lanes holding digit d OR their bit into the warp's mask
-    // word for d (a commutative update, so the mask is exact whatever order the lanes run in),
-    // read it back with the warp's running count of d, and the lowest lane of the group
-    // advances the count and clears the mask for the next item
+    // word for d (a commutative update, so the mask is exact whatever order the lanes run in) and
+    // read it back; the lowest lane of the group advances the warp's running count of d with one
+    // returning atomic, clears the mask for the next item, and hands the old count to its peers
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const uint32_t d = dr[i];
         atomicOr(wmask + d, 1u << lane);
         __syncwarp();
         const uint32_t peers = wmask[d];
-        const uint32_t before = wcnt[d];
         __syncwarp();
         const uint32_t lower = uint32_t(__popc(peers & ltmask));
+        uint32_t before = 0;
         if (lower == 0) {
-            wcnt[d] = before + uint32_t(__popc(peers));
+            before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
             wmask[d] = 0u;
         }
-        __syncwarp();
+        __syncwarp();          // the cleared masks are visible to the next item's updates
+        before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
         dr[i] = ((before + lower) << 8) | d;
     }
     __syncthreads();
