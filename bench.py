@@ -12,7 +12,9 @@ value      device-resident throughput: keys sorted per second over the K timed s
            (inputs already in HBM, radixsortcopynoalloc with preallocated buffers; every input
            is larger than the 129 MB L2, so no flush is needed between steps);
 e2e        the same sorts through the C ABI from pinned HOST buffers: each step copies the
-           inputs host->device, sorts, and copies the sorted arrays back;
+           inputs host->device, sorts, and copies the sorted arrays back (one stream per array,
+           so the copy engines move one array while another is sorted; the plain serial
+           sequence is reported beside it);
 roofline   the dominant kernel (the onesweep scatter pass on 64-bit keys): algorithmic bytes per
            launch (2 x 8 B x 2^28: read + write of one pass) / its average launch time, measured
            with CUDA events on the launch stream inside the timed region, against the measured
@@ -363,38 +365,69 @@ def uniform_u32(args, rs, dev, stream, peak) -> dict:
 
 
 def e2e_arm(args, rs, arrays, stream) -> dict:
-    """Host buffers in, host buffers out, through the C ABI: H2D + sort + D2H every step."""
+    """Host buffers in, host buffers out, through the C ABI: every step copies each array's keys
+    from pinned host memory, sorts them (radixsortcopynoalloc) and copies the result back.
+
+    Pipelined (the headline): each array of each step runs H2D -> sort -> D2H on its own stream,
+    with two sets of device buffers used by alternate steps, so the copy engines move one array
+    while the SMs sort another.  Serial: the same calls one after another on one stream."""
     import torch
     steps = max(1, min(args.steps, 5))
+    dev = arrays[0][1].device
     host_in = [b.cpu().pin_memory() for _, b, *_ in arrays]
-    host_out = [torch.empty_like(h).pin_memory() for h in host_in]
-    dev_in = [torch.empty_like(b) for _, b, *_ in arrays]
-    dev_out = [torch.empty_like(b) for _, b, *_ in arrays]
-    dev_buf = [torch.empty_like(b) for _, b, *_ in arrays]
     n = arrays[0][1].numel()
-    scr = [torch.empty(rs.scratch_bytes(kdt, n, d, m), dtype=torch.uint8, device=b.device)
-           for _, b, kdt, d, m in arrays]
     h2d = sum(h.numel() * h.element_size() for h in host_in)
+    slots = []
+    for _ in range(2):
+        slots.append({
+            "in": [torch.empty_like(b) for _, b, *_ in arrays],
+            "out": [torch.empty_like(b) for _, b, *_ in arrays],
+            "buf": [torch.empty_like(b) for _, b, *_ in arrays],
+            "scr": [torch.empty(rs.scratch_bytes(kdt, n, d, m), dtype=torch.uint8, device=dev)
+                    for _, b, kdt, d, m in arrays],
+            "host_out": [torch.empty_like(h).pin_memory() for h in host_in],
+            "streams": [torch.cuda.Stream(device=dev) for _ in arrays],
+        })
 
-    def one():
+    def one(slot, st=None):
         for i, (nm, b, kdt, d, m) in enumerate(arrays):
-            dev_in[i].copy_(host_in[i], non_blocking=True)
-            rs.radixsortcopynoalloc(dev_in[i], dev_out[i], dev_buf[i], scr[i], d, m, key_dtype=kdt, stream=stream)
-            host_out[i].copy_(dev_out[i], non_blocking=True)
+            s = st if st is not None else slot["streams"][i]
+            with torch.cuda.stream(s):
+                slot["in"][i].copy_(host_in[i], non_blocking=True)
+                rs.radixsortcopynoalloc(slot["in"][i], slot["out"][i], slot["buf"][i], slot["scr"][i], d, m,
+                                        key_dtype=kdt, stream=s)
+                slot["host_out"][i].copy_(slot["out"][i], non_blocking=True)
 
-    with torch.cuda.stream(stream):
-        one()
+    def timed(pipelined: bool) -> float:
+        one(slots[0], None if pipelined else stream)
         torch.cuda.synchronize()
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0.record(stream)
-        for _ in range(steps):
-            one()
+        if pipelined:
+            for sl in slots:
+                for s in sl["streams"]:
+                    s.wait_stream(stream)
+        for k in range(steps):
+            one(slots[k % 2], None if pipelined else stream)
+        if pipelined:
+            for sl in slots:
+                for s in sl["streams"]:
+                    stream.wait_stream(s)
         t1.record(stream)
-    torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1) / steps
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
+
+    ms_serial = timed(False)
+    ms = timed(True)
+    last = slots[(steps - 1) % 2]
+    same = all(torch.equal(last["host_out"][i], last["out"][i].cpu()) for i in range(len(arrays)))
     return {"value": round(3 * n / (ms * 1e-3) / 1e9, 3), "unit": "GKeys/s", "ms_per_step": round(ms, 3),
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "steps": steps,
-            "path": "pinned host -> cudaMemcpyAsync -> radixsortcopynoalloc -> cudaMemcpyAsync -> pinned host"}
+            "path": "pinned host -> cudaMemcpyAsync -> radixsortcopynoalloc -> cudaMemcpyAsync -> pinned host; "
+                    "one stream per array, two buffer sets for alternate steps (copies overlap other sorts)",
+            "serial": {"value": round(3 * n / (ms_serial * 1e-3) / 1e9, 3), "ms_per_step": round(ms_serial, 3),
+                       "path": "the same calls in order on one stream"},
+            "host_results_match_device": bool(same)}
 
 
 def cpu_sample_arrays(log2n_sample: int):
