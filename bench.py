@@ -419,6 +419,30 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
 
     ms_serial = timed(False)
     ms = timed(True)
+
+    def copy_gbps(h2d_on: bool, d2h_on: bool) -> float:
+        """Copy-engine bandwidth alone (same buffers, one stream per direction), GB/s."""
+        sa, sb = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        sa.wait_stream(stream)
+        sb.wait_stream(stream)
+        for i in range(len(arrays)):
+            if h2d_on:
+                with torch.cuda.stream(sa):
+                    slots[0]["in"][i].copy_(host_in[i], non_blocking=True)
+            if d2h_on:
+                with torch.cuda.stream(sb):
+                    slots[1]["host_out"][i].copy_(slots[1]["out"][i], non_blocking=True)
+        stream.wait_stream(sa)
+        stream.wait_stream(sb)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return round((h2d * (int(h2d_on) + int(d2h_on))) / (t0.elapsed_time(t1) * 1e-3) / 1e9, 1)
+
+    copies = {"h2d_alone_GBps": copy_gbps(True, False), "d2h_alone_GBps": copy_gbps(False, True),
+              "both_directions_GBps": copy_gbps(True, True)}
     last = slots[(steps - 1) % 2]
     same = all(torch.equal(last["host_out"][i], last["out"][i].cpu()) for i in range(len(arrays)))
     return {"value": round(3 * n / (ms * 1e-3) / 1e9, 3), "unit": "GKeys/s", "ms_per_step": round(ms, 3),
@@ -427,7 +451,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
                     "one stream per array, two buffer sets for alternate steps (copies overlap other sorts)",
             "serial": {"value": round(3 * n / (ms_serial * 1e-3) / 1e9, 3), "ms_per_step": round(ms_serial, 3),
                        "path": "the same calls in order on one stream"},
-            "host_results_match_device": bool(same)}
+            "host_results_match_device": bool(same), "copy_bandwidth": copies}
 
 
 def cpu_sample_arrays(log2n_sample: int):

@@ -1,9 +1,10 @@
 // rsbd8g_kernels.cuh - the sm_103a kernels of the stable LSD radix sort.
 //
-//   k_histogram / k_gather_histogram   all 256-bin digit histograms in one read of the keys,
-//                                      with warp-aggregated shared-memory atomics over several
-//                                      sub-histogram copies; the gather form reads the key through
-//                                      each object pointer and writes the filtered keys once
+//   k_histogram / k_gather_histogram   all 256-bin digit histograms in one read of the keys, with
+//                                      shared-memory atomics on per-lane-class counters (direct
+//                                      keys) or warp-aggregated atomics on sub-histogram copies
+//                                      (the gather form, which reads the key through each object
+//                                      pointer and writes the filtered keys once)
 //   k_plan                             exclusive scan of every digit histogram, the reference's
 //                                      pass-skip test, and the ping-pong plan of the passes
 //   k_onesweep                         one stable scatter pass of a surviving digit: persistent
@@ -21,8 +22,8 @@ namespace rsbd8g {
 
 // ---- up-front histograms --------------------------------------------------------------------
 
-// Histogram counting: each CTA keeps kHistCopies sub-histograms (P digits x 256 bins, u32) in
-// shared memory and its warps spread over them, so warps rarely collide on a bin.  A warp whose
+// Gather-histogram counting: each CTA keeps kHistCopies sub-histograms (P digits x 256 bins, u32)
+// in shared memory and its warps spread over them, so warps rarely collide on a bin.  A warp whose
 // lanes all share the digit (a skewed digit, e.g. the zero top bytes of small keys) adds 32 with
 // one atomic instead of 32 conflicting ones.
 constexpr int kHistCopies = 4;
@@ -60,53 +61,65 @@ __device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long lon
     }
 }
 
+// Direct keys: all P digit histograms in one read.  Every (digit position, bin) has C shared-memory
+// counters, one per lane class (lane % C), laid out so that lane l always uses bank l % 32: the 32
+// lanes of a warp never meet in a bank (C = 32, keys up to 4 bytes) or at most pairwise (C = 16,
+// 8-byte keys, 128 KB either way).  One 1024-thread CTA per SM reads 16-byte vectors grid-strided;
+// at the end each CTA folds its C copies (rotated reads, conflict-free) into the global histogram.
+template <int P>
+constexpr int hist_lane_copies() { return P <= 4 ? 32 : 16; }
+
 template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, uint32_t dmask,
                                                        unsigned long long *__restrict__ ghist) {
     constexpr int P = int(sizeof(U));
+    constexpr int C = hist_lane_copies<P>();
     constexpr int V = 16 / int(sizeof(U));
-    __shared__ uint32_t shall[kHistCopies * P * kBuckets];
-    zero_hist<THREADS, P>(shall);
-    uint32_t *sh = shall + ((threadIdx.x >> 5) % kHistCopies) * P * kBuckets;
+    extern __shared__ __align__(16) uint32_t shl[];
+    for (int i = threadIdx.x; i < C * P * kBuckets; i += THREADS) shl[i] = 0;
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
-    // scalar head up to 16-byte alignment, vector body, scalar tail
+    uint32_t *sh = shl + (lane & uint32_t(C - 1));
+    auto count = [&](U k, bool ok) {
+        if (!ok) return;
+#pragma unroll
+        for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dmask)) * C, 1u);
+    };
     const uint64_t mis = (reinterpret_cast<uintptr_t>(keys) & 15u) / sizeof(U);
     const uint64_t head = mis ? (uint64_t(V) - mis < n ? uint64_t(V) - mis : n) : 0;
     const uint64_t nvec = (n - head) / V;
     const uint64_t tail0 = head + nvec * V;
-    const uint64_t gwarp = (uint64_t(blockIdx.x) * THREADS + threadIdx.x) >> 5;
-    const uint64_t nwarps = (uint64_t(gridDim.x) * THREADS) >> 5;
-    if (gwarp == 0) {  // head and tail by the first warp of the grid
-        for (uint64_t b = 0; b < head; b += 32) {
-            const uint64_t i = b + lane;
-            const bool ok = i < head;
-            count_key(sh, filter_key<MODE>(ok ? keys[i] : U(0)), ok, dmask);
-        }
-        for (uint64_t b = tail0; b < n; b += 32) {
-            const uint64_t i = b + lane;
-            const bool ok = i < n;
-            count_key(sh, filter_key<MODE>(ok ? keys[i] : U(0)), ok, dmask);
-        }
+    const uint64_t gthread = uint64_t(blockIdx.x) * THREADS + threadIdx.x;
+    const uint64_t nthreads = uint64_t(gridDim.x) * THREADS;
+    if (gthread < 32) {
+        for (uint64_t i = gthread; i < head; i += 32) count(filter_key<MODE>(keys[i]), true);
+        for (uint64_t i = tail0 + gthread; i < n; i += 32) count(filter_key<MODE>(keys[i]), true);
     }
     const uint4 *kv = reinterpret_cast<const uint4 *>(keys + head);
     constexpr int UNR = 4;
-    for (uint64_t b = gwarp * 32 * UNR; b < nvec; b += nwarps * 32 * UNR) {
+    for (uint64_t b = gthread; b < nvec; b += nthreads * UNR) {
         uint4 v[UNR];
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
-            const uint64_t i = b + u * 32 + lane;
+            const uint64_t i = b + uint64_t(u) * nthreads;
             v[u] = i < nvec ? __ldg(kv + i) : make_uint4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
-            const bool ok = b + u * 32 + lane < nvec;
+            const bool ok = b + uint64_t(u) * nthreads < nvec;
             U k[V];
             memcpy(k, &v[u], 16);
 #pragma unroll
-            for (int j = 0; j < V; ++j) count_key(sh, filter_key<MODE>(k[j]), ok, dmask);
+            for (int j = 0; j < V; ++j) count(filter_key<MODE>(k[j]), ok);
         }
     }
-    flush_hist<THREADS, P>(shall, ghist);
+    __syncthreads();
+    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
+        uint32_t t = 0;
+#pragma unroll 8
+        for (int c = 0; c < C; ++c) t += shl[i * C + ((c + i) & (C - 1))];
+        if (t) atomicAdd(ghist + i, (unsigned long long)t);
+    }
 }
 
 // indirect form: gather the key through each object pointer (level 1: at off1; level 2: behind the

@@ -14,7 +14,8 @@
 
 namespace rsbd8g {
 
-constexpr int kHistThreads = 512;
+constexpr int kHistThreads = 512;         // gather histogram (indirect keys)
+constexpr int kHistDirectThreads = 1024;  // direct keys: one CTA per SM
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch, uint32_t dmask,
@@ -58,7 +59,14 @@ cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, co
             static_cast<const uint64_t *>(in), n, dmask, r.off1, r.off2, int(r.indirect),
             static_cast<const U *>(r.keys), reinterpret_cast<U *>(scratch + L.keys_a), ghist);
     } else {
-        k_histogram<U, MODE, kHistThreads><<<grid, kHistThreads, 0, s>>>(static_cast<const U *>(in), n, dmask, ghist);
+        constexpr size_t smem = size_t(hist_lane_copies<int(sizeof(U))>()) * sizeof(U) * kBuckets * 4;
+        auto kern = k_histogram<U, MODE, kHistDirectThreads>;
+        static std::once_flag once[64];
+        std::call_once(once[dev & 63],
+                       [&] { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); });
+        const uint64_t per = uint64_t(kHistDirectThreads) * 64;
+        const uint32_t g = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per - 1) / per, device_sms(dev))));
+        kern<<<g, kHistDirectThreads, smem, s>>>(static_cast<const U *>(in), n, dmask, ghist);
     }
     return cudaGetLastError();
 }
