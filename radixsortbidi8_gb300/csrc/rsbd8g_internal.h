@@ -59,7 +59,7 @@ struct SweepGeometry {
     int threads, items;
 };
 constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
-    return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 12 : 16};
+    return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 16 : 24};
 }
 
 #define RSBD8G_MODE_SWITCH(mode, CALL) \

@@ -90,7 +90,12 @@ cudaError_t launch_segmented_mode_t(const Resolved &r, const SegArgs &a, const S
     if (e != cudaSuccess) return e;
     {
         LaunchTimer t(s, RSBD8G_KERNEL_HISTOGRAM, uint32_t(sizeof(U)), 0, a.nsegs);
-        k_seg_hist<U, MODE, 512><<<uint32_t(sms) * 4, 512, 0, s>>>(a, in);
+        constexpr size_t smem = size_t(hist_lane_copies<int(sizeof(U))>()) * sizeof(U) * kBuckets * 4;
+        auto kern = k_seg_hist<U, MODE, 1024>;
+        static std::once_flag once[64];
+        std::call_once(once[dev & 63],
+                       [&] { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); });
+        kern<<<uint32_t(sms), 1024, smem, s>>>(a, in);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     {

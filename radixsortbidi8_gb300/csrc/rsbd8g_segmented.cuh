@@ -146,7 +146,8 @@ __device__ __forceinline__ uint32_t seg_of_tile(const uint32_t *tbase, uint32_t 
 template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__restrict__ in) {
     constexpr int P = int(sizeof(U));
-    __shared__ uint32_t sh[P * kBuckets];
+    constexpr int C = hist_lane_copies<P>();
+    extern __shared__ __align__(16) uint32_t shl[];   // C lane-class copies, as in k_histogram
     const SegControl *c = a.ctrl;
     if (c->abort) return;
     const uint32_t T = c->ntiles, nl = c->nlarge;
@@ -154,8 +155,9 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
     const uint32_t t0 = uint32_t(uint64_t(T) * blockIdx.x / gridDim.x);
     const uint32_t t1 = uint32_t(uint64_t(T) * (blockIdx.x + 1) / gridDim.x);
     if (t0 >= t1) return;
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) sh[i] = 0;
+    for (int i = threadIdx.x; i < C * P * kBuckets; i += THREADS) shl[i] = 0;
     __syncthreads();
+    uint32_t *sh = shl + (threadIdx.x & uint32_t(C - 1));
     uint32_t idx = seg_of_tile(a.large_tbase, nl, t0);
     for (uint32_t gt = t0; gt < t1;) {
         while (a.large_tbase[idx + 1] <= gt) ++idx;
@@ -165,18 +167,23 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
         const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
-        const uint32_t lane = threadIdx.x & 31u;
-        for (uint64_t b = k0 + (threadIdx.x & ~31u); b < k1; b += THREADS) {
-            const uint64_t i = b + lane;
-            const bool ok = i < k1;
-            count_key(sh, filter_key<MODE>(ok ? src[i] : U(0)), ok, a.dmask);
+        for (uint64_t i = k0 + threadIdx.x; i < k1; i += THREADS) {
+            const U k = filter_key<MODE>(src[i]);
+#pragma unroll
+            for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ a.dmask)) * C, 1u);
         }
         __syncthreads();
+        // fold the copies (rotated reads: conflict-free), clear them for the next segment
         uint32_t *gh = a.seg_hist + size_t(idx) * P * kBuckets;
         for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
-            const uint32_t v = sh[i];
+            uint32_t v = 0;
+#pragma unroll 8
+            for (int cc = 0; cc < C; ++cc) {
+                uint32_t *w = shl + i * C + ((cc + i) & (C - 1));
+                v += *w;
+                *w = 0;
+            }
             if (v) atomicAdd(gh + i, v);
-            sh[i] = 0;
         }
         __syncthreads();
         gt = tend;
