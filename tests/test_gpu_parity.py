@@ -16,7 +16,9 @@ pytestmark = pytest.mark.gpu
 DIRS = ["ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"]
 TYPES = [np.uint8, np.int8, np.uint16, np.int16, np.uint32, np.int32, np.float32,
          np.uint64, np.int64, np.float64]
-EDGE_SIZES = [2, 3, 31, 32, 33, 255, 256, 257, 4095, 4097, 8191, 8192, 8193, 16385, 65543]
+# around the scatter tiles: 12288 keys up to 4 bytes, 8192 for 8-byte keys, 4096 with a pointer payload
+EDGE_SIZES = [2, 3, 31, 32, 33, 255, 256, 257, 4095, 4096, 4097, 8191, 8192, 8193, 12287, 12288, 12289,
+              16385, 24575, 24577, 65543]
 ALL_MODES = ["native", "nativeabs", "nativetieredabs", "forceunsigned", "forcesigned", "forceabssigned",
              "forcefloatingp", "forceabsfloatingp", "specialfloatingp", "forcetieredabsfloatingp",
              "forcetieredabssigned"]
@@ -276,3 +278,20 @@ def test_indirect_second_level_and_inplace():
         p2 = ptrs.clone()
         assert rs.radixsort_member(p2, np.float32, 8, d, offset2=0)
         assert np.array_equal((p2.cpu().numpy() - hdev.data_ptr()) // 16, idx)
+
+
+@pytest.mark.parametrize("n", [2, 33, 4095, 4096, 4097, 8193])
+def test_indirect_tile_edges(n):
+    """Pointer-payload sorts around their 4096-key tiles, against the oracle."""
+    import torch
+    rs = R()
+    rec = S.records24(0x5EED0011, n)
+    raw, base = _records_dev(rec)
+    ptrs = torch.arange(n, dtype=torch.int64, device="cuda") * 24 + base
+    host_ptrs = np.uint64(rec.ctypes.data) + np.arange(n, dtype=np.uint64) * np.uint64(24)
+    for d in DIRS:
+        out = torch.empty_like(ptrs)
+        assert rs.radixsortcopy_member(ptrs, out, np.float64, 8, d)
+        idx = (out.cpu().numpy() - base) // 24
+        want = (O.sortcopy_indirect(host_ptrs, np.float64, 8, "native", d) - np.uint64(rec.ctypes.data)) // 24
+        assert np.array_equal(idx, want.astype(np.int64)), d
