@@ -64,7 +64,7 @@ cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, co
         static std::once_flag once[64];
         std::call_once(once[dev & 63],
                        [&] { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); });
-        const uint64_t per = uint64_t(kHistDirectThreads) * 64;
+        const uint64_t per = uint64_t(kHistDirectThreads) * 16;   // at least 16 keys a thread
         const uint32_t g = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per - 1) / per, device_sms(dev))));
         kern<<<g, kHistDirectThreads, smem, s>>>(static_cast<const U *>(in), n, dmask, ghist);
     }
