@@ -61,6 +61,9 @@ struct SweepGeometry {
 constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
     return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 16 : 24};
 }
+// the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
+// segment's last tile is partly empty, and large 8-byte segments are the shorter ones)
+constexpr SweepGeometry seg_sweep_geometry(int key_bytes) { return SweepGeometry{512, key_bytes == 8 ? 12 : 24}; }
 
 #define RSBD8G_MODE_SWITCH(mode, CALL) \
     switch (mode) {                    \

@@ -104,7 +104,7 @@ cudaError_t launch_segmented_mode_t(const Resolved &r, const SegArgs &a, const S
         k_seg_plan<<<g, 256, 0, s>>>(a, int(sizeof(U)));
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    constexpr SweepGeometry gd = sweep_geometry(int(sizeof(U)), false);
+    constexpr SweepGeometry gd = seg_sweep_geometry(int(sizeof(U)));
     const uint32_t stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 1u : 0xFFFFFFFFu;
     e = launch_seg_sweeps_t<U, MODE, gd.threads, gd.items>(a, L, scratch, in, out, buf, stall, s);
     if (e != cudaSuccess) return e;

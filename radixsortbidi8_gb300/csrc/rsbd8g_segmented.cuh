@@ -167,10 +167,21 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
         const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
-        for (uint64_t i = k0 + threadIdx.x; i < k1; i += THREADS) {
-            const U k = filter_key<MODE>(src[i]);
+        constexpr int UNR = 8;                           // loads in flight per thread
+        for (uint64_t b = k0 + threadIdx.x; b < k1; b += uint64_t(THREADS) * UNR) {
+            U raw[UNR];
 #pragma unroll
-            for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ a.dmask)) * C, 1u);
+            for (int u = 0; u < UNR; ++u) {
+                const uint64_t i = b + uint64_t(u) * THREADS;
+                raw[u] = i < k1 ? src[i] : U(0);
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                if (b + uint64_t(u) * THREADS >= k1) break;
+                const U k = filter_key<MODE>(raw[u]);
+#pragma unroll
+                for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ a.dmask)) * C, 1u);
+            }
         }
         __syncthreads();
         // fold the copies (rotated reads: conflict-free), clear them for the next segment

@@ -22,7 +22,7 @@ rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, cons
     const uint32_t cap = uint32_t(sh.threads * sh.items);
     const uint32_t cutoff = (t && t->small_cutoff) ? t->small_cutoff : cap;
     if (cutoff > cap) return RSBD8G_ERR_BAD_ARG;
-    const SweepGeometry g = sweep_geometry(int(r.key_bytes), false);
+    const SweepGeometry g = seg_sweep_geometry(int(r.key_bytes));
     L->tile = uint32_t(g.threads * g.items);
     L->cutoff = cutoff;
     L->small_variant = variant;
