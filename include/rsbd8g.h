@@ -49,8 +49,14 @@ typedef enum rsbd8g_status {
 } rsbd8g_status;
 
 /* what std::is_signed_v / std::is_floating_point_v report for the key type:
- * enumerations, bool and classes are RSBD8G_KIND_UNSIGNED, as in the reference */
-enum { RSBD8G_KIND_UNSIGNED = 0, RSBD8G_KIND_SIGNED = 1, RSBD8G_KIND_FLOAT = 2 };
+ * enumerations, bool and classes are RSBD8G_KIND_UNSIGNED, as in the reference.
+ * 16-byte keys (two little-endian 64-bit words, 16-byte aligned arrays): UNSIGNED / SIGNED for
+ * 128-bit integers, FLOAT for a 128-bit float word with the sign in bit 127 (IEEE binary128, the
+ * reference's test128 with the floating-point flag), and RSBD8G_KIND_X87 for x87 extended
+ * precision in 16-byte storage (64-bit significand, then sign and 15-bit exponent; the upper
+ * 48 bits are padding, ignored by the order and moved with the element: the reference's
+ * longdoubletest128, and long double on x86-64) */
+enum { RSBD8G_KIND_UNSIGNED = 0, RSBD8G_KIND_SIGNED = 1, RSBD8G_KIND_FLOAT = 2, RSBD8G_KIND_X87 = 3 };
 
 /* rsbd8::sortingmode values (Radixsortbidi8.hpp:212-250) */
 enum {
@@ -84,7 +90,7 @@ enum {
 #define RSBD8G_FLAG_DIAG_STALL 1u
 
 typedef struct rsbd8g_desc {
-    uint32_t key_bytes;     /* 1, 2, 4 or 8 */
+    uint32_t key_bytes;     /* 1, 2, 4, 8 or 16 (16: not in the segmented and serving entry points) */
     uint32_t key_kind;      /* RSBD8G_KIND_* */
     uint32_t mode;          /* rsbd8::sortingmode value */
     uint32_t direction;     /* rsbd8::sortingdirection value */

@@ -209,6 +209,103 @@ def numpy_sort_indices(keys: np.ndarray, mode="native", direction="ascfwdorder",
     return idx[np.argsort(k, kind="stable")]
 
 
+# ---- 16-byte keys -------------------------------------------------------------------
+# Arrays of 16-byte keys are (n, 2) uint64 arrays of little-endian words [lo, hi].  Kinds:
+#   "u128" / "i128"  128-bit integers (the reference's test128 without / with the sign flag),
+#   "f128"           a 128-bit float word, sign in bit 127 (test128 with the float flags),
+#   "x87"            x87 extended precision in 16-byte storage: 80-bit key, sign in bit 79; the
+#                    upper 48 bits of `hi` are padding (longdoubletest128, Radixsortbidi8.hpp:1061-1100).
+
+WIDE_KINDS = {"u128": (KIND_UNSIGNED, 64), "i128": (KIND_SIGNED, 64), "f128": (KIND_FLOAT, 64),
+              "x87": (KIND_FLOAT, 16)}
+
+
+def resolve_wide(kind: str, mode="native", direction="ascfwdorder", indirect: int = 0) -> Desc:
+    k, _ = WIDE_KINDS[kind]
+    d = Desc()
+    if lib().rsbd8o_resolve(k, _mode(mode), _dir(direction), indirect, ctypes.byref(d)) != 0:
+        raise ValueError(f"bad mode/direction {mode!r}/{direction!r}")
+    d.key_bytes = 16
+    return d
+
+
+def sortkeys_wide(words: np.ndarray, kind: str, d: Desc) -> tuple[np.ndarray, np.ndarray]:
+    """K(b) of 16-byte keys as (lo, hi) uint64 arrays: the 8 filter combinations of the
+    (64 + HB)-bit key, the same formulas as sortkeys on narrower keys, with a carry between words."""
+    hb = WIDE_KINDS[kind][1]
+    u = np.uint64
+    hm = u((1 << hb) - 1) if hb < 64 else u(0xFFFFFFFFFFFFFFFF)
+    sb = u(1 << (hb - 1))
+    lo = words[:, 0].astype(u)
+    hi = words[:, 1].astype(u) & hm
+    s = (hi & sb) != 0
+    sm = np.where(s, u(0xFFFFFFFFFFFFFFFF), u(0))
+
+    def add_s(l, h):                      # (l, h) + (sm, sm): subtract 1 where negative
+        r = l + sm
+        c = (r < l).astype(u)
+        return r, (h + sm + c) & hm
+
+    def shl1(l, h):
+        return l << u(1), ((h << u(1)) | (l >> u(63))) & hm
+
+    with np.errstate(over="ignore"):
+        if d.absv != d.fltp:
+            if d.absv:
+                kl, kh = add_s(lo, hi) if d.sign else shl1(lo, hi)
+                kl, kh = kl ^ sm, (kh ^ sm) & hm
+            else:
+                mh = hi & ~sb
+                if d.sign:
+                    kl, kh = add_s(lo, mh)
+                    kl, kh = kl ^ sm, ((kh ^ sm) & hm) ^ sb
+                else:
+                    kl, kh = lo ^ sm, (mh ^ sm) & hm
+        elif d.absv:
+            if d.sign:
+                kl, kh = lo, hi & ~sb
+            else:
+                kl, kh = shl1(lo, hi)
+                kl = (kl | (hi >> u(hb - 1))) ^ u(1)
+        else:
+            kl, kh = (lo, hi ^ sb) if d.sign else (lo, hi)
+        if d.desc:
+            kl, kh = ~kl, ~kh & hm
+    return kl, kh
+
+
+def sortcopy_wide(words: np.ndarray, kind: str, mode="native", direction="ascfwdorder") -> np.ndarray:
+    """Stable sort of 16-byte keys ((n, 2) uint64 words), as rsbd8::radixsortcopy<direction, mode>."""
+    words = np.ascontiguousarray(words, dtype=np.uint64).reshape(-1, 2)
+    d = resolve_wide(kind, mode, direction)
+    src = words[::-1] if d.rev else words
+    kl, kh = sortkeys_wide(src, kind, d)
+    return src[np.lexsort((kl, kh))]            # lexsort is stable; the last key is the primary one
+
+
+def sort_indices_wide(words: np.ndarray, kind: str, mode="native", direction="ascfwdorder") -> np.ndarray:
+    """Permutation the indirect sort applies to objects whose 16-byte keys are `words` (pointer order)."""
+    words = np.ascontiguousarray(words, dtype=np.uint64).reshape(-1, 2)
+    d = resolve_wide(kind, mode, direction, indirect=1)
+    n = words.shape[0]
+    idx = np.arange(n)[::-1] if d.rev else np.arange(n)
+    kl, kh = sortkeys_wide(words[idx], kind, d)
+    return idx[np.lexsort((kl, kh))]
+
+
+def ref_sortcopy_wide(words: np.ndarray, kind: str, mode, direction) -> np.ndarray:
+    """The reference's own radixsortcopy on 16-byte keys (16-byte class under a forced mode, or
+    long double as x87); KeyError where that combination is not instantiated."""
+    words = np.ascontiguousarray(words, dtype=np.uint64).reshape(-1, 2)
+    tn = "x87" if kind == "x87" else "w128"
+    f = _reffn(f"rsbd8ref_copy_{tn}_m{_mode(mode)}_d{_dir(direction)}")
+    out = np.zeros_like(words)
+    rc = f(ctypes.c_uint64(words.shape[0]), ctypes.c_void_p(words.ctypes.data), ctypes.c_void_p(out.ctypes.data))
+    if rc != 0:
+        raise RuntimeError(f"reference sort failed ({rc})")
+    return out
+
+
 # ---- the reference's own sort (only where it was compiled) -------------------------
 
 def ref_available() -> bool:

@@ -38,6 +38,10 @@ template<sortingdirection D, sortingmode M, typename T>
 int indirect_impl(std::uint64_t n, void const *in, void *out) {
 	return rsbd8::radixsortcopy<T, 8, D, M>(n, static_cast<rec24 *const *>(in), static_cast<rec24 **>(out)) ? 0 : -2;
 }
+// 16-byte key as a plain class: two little-endian 64-bit words
+struct k128 { std::uint64_t lo, hi; };
+static_assert(sizeof(k128) == 16);
+static_assert(sizeof(long double) == 16, "x86-64 long double: x87 extended precision in 16 bytes");
 template<sortingdirection D>
 int member_impl(std::uint64_t n, void const *in, void *out) {
 	return rsbd8::radixsortcopy<&rec24::key, D>(n, static_cast<rec24 *const *>(in), static_cast<rec24 **>(out)) ? 0 : -2;
@@ -102,6 +106,16 @@ RSBD8REF_DIRS(RSBD8REF_INPLACE, float, f32, native, 64)
 RSBD8REF_DIRS(RSBD8REF_INPLACE, std::int64_t, i64, native, 64)
 RSBD8REF_DIRS(RSBD8REF_INPLACE, double, f64, native, 64)
 RSBD8REF_DIRS(RSBD8REF_INPLACE, std::int16_t, i16, native, 64)
+#elif REF_PART == 7
+// 16-byte keys: a 16-byte class (two little-endian 64-bit words; the reference's test128 with
+// the mode bits of the call) under the sound forced modes, and long double (x87 extended
+// precision in 16-byte storage on x86-64: the reference's longdoubletest128)
+RSBD8REF_DIRS(RSBD8REF_COPY, k128, w128, forceunsigned, 0)
+RSBD8REF_DIRS(RSBD8REF_COPY, k128, w128, forcetieredabssigned, 1)
+RSBD8REF_DIRS(RSBD8REF_COPY, k128, w128, forcesigned, 2)
+RSBD8REF_DIRS(RSBD8REF_COPY, k128, w128, specialfloatingp, 4)
+RSBD8REF_DIRS(RSBD8REF_COPY, k128, w128, forcefloatingp, 6)
+RSBD8REF_DIRS(RSBD8REF_COPY, long double, x87, native, 64)
 #else
-#error "REF_PART must be 0..6"
+#error "REF_PART must be 0..7"
 #endif

@@ -30,7 +30,9 @@ MODES = {
 }
 DIRECTIONS = {"ascfwdorder": 0, "dscfwdorder": 1, "ascrevorder": 2, "dscrevorder": 3}
 
-KIND_UNSIGNED, KIND_SIGNED, KIND_FLOAT = 0, 1, 2
+KIND_UNSIGNED, KIND_SIGNED, KIND_FLOAT, KIND_X87 = 0, 1, 2, 3
+# 16-byte keys (arrays of two little-endian 64-bit words per key, 16-byte aligned): named by string
+WIDE_KEY_KINDS = {"u128": KIND_UNSIGNED, "i128": KIND_SIGNED, "f128": KIND_FLOAT, "x87": KIND_X87}
 DIRECT, MEMBER, MEMBER2 = 0, 1, 2
 FLAG_DIAG_STALL = 1
 
@@ -128,7 +130,11 @@ def _np_dtype(dt) -> np.dtype:
 
 
 def key_kind(dtype) -> tuple[int, int]:
-    """(kind, key bytes): what std::is_signed_v / is_floating_point_v say of the key type."""
+    """(kind, key bytes): what std::is_signed_v / is_floating_point_v say of the key type.
+    16-byte keys are named "u128", "i128", "f128" (a 128-bit float word) or "x87" (x87 extended
+    precision in 16-byte storage)."""
+    if isinstance(dtype, str) and dtype in WIDE_KEY_KINDS:
+        return WIDE_KEY_KINDS[dtype], 16
     dt = _np_dtype(dtype)
     if dt == np.bool_:
         return KIND_UNSIGNED, 1
@@ -183,9 +189,11 @@ def _check(st: int, what: str) -> None:
         raise RSBD8GError(st, what)
 
 
-def _count(x, count):
+def _count(x, count, desc=None):
     if count is not None:
         return int(count)
+    if desc is not None and desc.indirection == DIRECT and desc.key_bytes == 16:
+        return int(x.numel() * x.element_size() // 16)       # 16-byte keys held in a wider-typed tensor
     return int(x.numel())
 
 
@@ -205,7 +213,7 @@ def radixsortcopy(input, output, direction="ascfwdorder", mode="native", key_dty
     """rsbd8::radixsortcopy<direction, mode>(count, input, output): True when sorted, False when
     the device allocation failed (the reference's only false return)."""
     d = make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode, flags=flags)
-    st = lib().rsbd8g_radixsortcopy(ctypes.byref(d), _count(input, count), _ptr(input), _ptr(output),
+    st = lib().rsbd8g_radixsortcopy(ctypes.byref(d), _count(input, count, d), _ptr(input), _ptr(output),
                                     _stream(stream))
     if st == ERR_NO_MEMORY:
         return False
@@ -217,7 +225,7 @@ def radixsort(input, direction="ascfwdorder", mode="native", key_dtype=None, cou
               flags: int = 0) -> bool:
     """rsbd8::radixsort<direction, mode>(count, input): in-place sort."""
     d = make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode, flags=flags)
-    st = lib().rsbd8g_radixsort(ctypes.byref(d), _count(input, count), _ptr(input), _stream(stream))
+    st = lib().rsbd8g_radixsort(ctypes.byref(d), _count(input, count, d), _ptr(input), _stream(stream))
     if st == ERR_NO_MEMORY:
         return False
     _check(st, "radixsort")
@@ -229,7 +237,7 @@ def radixsortcopynoalloc(input, output, buffer, scratch, direction="ascfwdorder"
     """rsbd8::radixsortcopynoalloc: caller buffer + scratch (a uint8 CUDA tensor), stream-ordered."""
     d = make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode, flags=flags)
     nbytes = scratch_bytes_ if scratch_bytes_ is not None else scratch.numel() * scratch.element_size()
-    _check(lib().rsbd8g_radixsortcopynoalloc(ctypes.byref(d), _count(input, count), _ptr(scratch), nbytes,
+    _check(lib().rsbd8g_radixsortcopynoalloc(ctypes.byref(d), _count(input, count, d), _ptr(scratch), nbytes,
                                              _ptr(input), _ptr(output), _ptr(buffer), _stream(stream)),
            "radixsortcopynoalloc")
 
@@ -240,7 +248,7 @@ def radixsortnoalloc(input, buffer, scratch, movetobuffer: bool = False, directi
     """rsbd8::radixsortnoalloc: in place (or into buffer with movetobuffer), stream-ordered."""
     d = make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode, flags=flags)
     nbytes = scratch_bytes_ if scratch_bytes_ is not None else scratch.numel() * scratch.element_size()
-    _check(lib().rsbd8g_radixsortnoalloc(ctypes.byref(d), _count(input, count), _ptr(scratch), nbytes,
+    _check(lib().rsbd8g_radixsortnoalloc(ctypes.byref(d), _count(input, count, d), _ptr(scratch), nbytes,
                                          _ptr(input), _ptr(buffer), int(bool(movetobuffer)), _stream(stream)),
            "radixsortnoalloc")
 
@@ -260,7 +268,7 @@ def radixsortcopy_member(input, output, key_dtype, offset: int, direction="ascfw
     behind it).  input/output are uint64/int64 CUDA tensors of device addresses."""
     ind = MEMBER if offset2 is None else MEMBER2
     d = make_desc(key_dtype, direction, mode, ind, offset, offset2 or 0, flags)
-    st = lib().rsbd8g_radixsortcopy(ctypes.byref(d), _count(input, count), _ptr(input), _ptr(output),
+    st = lib().rsbd8g_radixsortcopy(ctypes.byref(d), _count(input, count, d), _ptr(input), _ptr(output),
                                     _stream(stream))
     if st == ERR_NO_MEMORY:
         return False
@@ -273,7 +281,7 @@ def radixsort_member(input, key_dtype, offset: int, direction="ascfwdorder", mod
     """rsbd8::radixsort<T, offset, direction, mode>: in-place sort of object addresses."""
     ind = MEMBER if offset2 is None else MEMBER2
     d = make_desc(key_dtype, direction, mode, ind, offset, offset2 or 0)
-    st = lib().rsbd8g_radixsort(ctypes.byref(d), _count(input, count), _ptr(input), _stream(stream))
+    st = lib().rsbd8g_radixsort(ctypes.byref(d), _count(input, count, d), _ptr(input), _stream(stream))
     if st == ERR_NO_MEMORY:
         return False
     _check(st, "radixsort (indirection)")
@@ -285,7 +293,7 @@ def radixsortcopynoalloc_member(input, output, buffer, scratch, key_dtype, offse
     ind = MEMBER if offset2 is None else MEMBER2
     d = make_desc(key_dtype, direction, mode, ind, offset, offset2 or 0)
     nbytes = scratch.numel() * scratch.element_size()
-    _check(lib().rsbd8g_radixsortcopynoalloc(ctypes.byref(d), _count(input, count), _ptr(scratch), nbytes,
+    _check(lib().rsbd8g_radixsortcopynoalloc(ctypes.byref(d), _count(input, count, d), _ptr(scratch), nbytes,
                                              _ptr(input), _ptr(output), _ptr(buffer), _stream(stream)),
            "radixsortcopynoalloc (indirection)")
 

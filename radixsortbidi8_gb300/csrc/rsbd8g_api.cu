@@ -135,15 +135,17 @@ rsbd8g_status profile_collect(rsbd8g_launch_record *out, size_t cap, size_t *cou
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
     if (!d || !r) return RSBD8G_ERR_BAD_ARG;
-    if (d->key_bytes != 1 && d->key_bytes != 2 && d->key_bytes != 4 && d->key_bytes != 8) return RSBD8G_ERR_BAD_ARG;
-    if (d->key_kind > RSBD8G_KIND_FLOAT) return RSBD8G_ERR_BAD_ARG;
-    if (d->key_kind == RSBD8G_KIND_FLOAT && d->key_bytes < 4) return RSBD8G_ERR_BAD_ARG;
+    const uint32_t kb = d->key_bytes;
+    if (kb != 1 && kb != 2 && kb != 4 && kb != 8 && kb != 16) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_kind > RSBD8G_KIND_X87) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_kind == RSBD8G_KIND_FLOAT && kb < 4) return RSBD8G_ERR_BAD_ARG;
+    if (d->key_kind == RSBD8G_KIND_X87 && kb != 16) return RSBD8G_ERR_BAD_ARG;
     const uint32_t mode = d->mode, dir = d->direction;
     if (!(mode < 8u || (mode >= 64u && mode <= 66u))) return RSBD8G_ERR_BAD_ARG;
     if (dir > 3u) return RSBD8G_ERR_BAD_ARG;
     if (d->indirection > RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
-    const bool is_signed = d->key_kind == RSBD8G_KIND_SIGNED || d->key_kind == RSBD8G_KIND_FLOAT;
-    const bool is_float = d->key_kind == RSBD8G_KIND_FLOAT;
+    const bool is_float = d->key_kind == RSBD8G_KIND_FLOAT || d->key_kind == RSBD8G_KIND_X87;
+    const bool is_signed = d->key_kind == RSBD8G_KIND_SIGNED || is_float;
     Filter f;
     f.absv = (mode >= 65u && is_signed) || (mode < 64u && (mode & 1u));
     f.sign = (mode >= 64u && mode <= 65u && is_signed) || (mode < 64u && (mode & 2u));
@@ -154,6 +156,8 @@ rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
     r->rev = d->indirection ? ((dir >> 1) & 1u)
                             : (((dir >> 1) & 1u) && ((f.absv && f.sign) || (!f.absv && f.sign && f.fltp)));
     r->key_bytes = d->key_bytes;
+    r->x87 = d->key_kind == RSBD8G_KIND_X87;
+    r->digits = r->x87 ? 10u : d->key_bytes;
     r->elem_bytes = d->indirection ? 8u : d->key_bytes;
     r->off1 = d->offset1;
     r->off2 = d->offset2;
@@ -169,7 +173,7 @@ Layout layout_for(const Resolved &r, uint64_t n) {
     L.num_tiles = uint32_t((n + tile - 1) / tile);
     L.wide_status = n >= kNarrowStatusLimit;
     const size_t sw = L.wide_status ? 8 : 4;
-    const uint32_t passes = r.key_bytes;
+    const uint32_t passes = r.digits;
     L.ctrl = 0;
     L.ghist = align_up(sizeof(Control));
     L.bstart = L.ghist + align_up(size_t(kMaxPasses) * kBuckets * 8);
@@ -190,12 +194,20 @@ rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t 
     if (!scratch || scratch_bytes < L.total) return RSBD8G_ERR_BAD_ARG;
     if ((reinterpret_cast<uintptr_t>(scratch) & (kAlign - 1)) != 0) return RSBD8G_ERR_BAD_ARG;
     unsigned char *sc = static_cast<unsigned char *>(scratch);
+    if (r.key_bytes == 16 && !r.indirect) {   // 16-byte keys move as aligned 16-byte words
+        auto mis = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; };
+        if (mis(in) || (out && mis(out)) || (buf && mis(buf))) return RSBD8G_ERR_BAD_ARG;
+    }
     cudaError_t e;
     switch (r.key_bytes) {
         case 1: e = launch_sort_k1(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
         case 2: e = launch_sort_k2(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
         case 4: e = launch_sort_k4(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
-        default: e = launch_sort_k8(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        case 8: e = launch_sort_k8(r, n, L, sc, in, out, buf, inplace, to_buffer, s); break;
+        default:
+            e = r.x87 ? launch_sort_x87(r, n, L, sc, in, out, buf, inplace, to_buffer, s)
+                      : launch_sort_k16(r, n, L, sc, in, out, buf, inplace, to_buffer, s);
+            break;
     }
     return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
 }
@@ -299,6 +311,34 @@ RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stre
     return read_device_status(scratch, reinterpret_cast<cudaStream_t>(stream), true);
 }
 
+// The allocating forms draw buffer + scratch from a library-owned stream-ordered pool per device
+// that keeps up to kPoolKeepBytes of freed memory mapped, so back-to-back sorts do not map (and
+// the driver does not unmap) hundreds of megabytes on every call; the process-wide default pool
+// is left as the application configured it.
+constexpr uint64_t kPoolKeepBytes = uint64_t(8) << 30;
+
+static cudaMemPool_t sort_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    static std::once_flag once[64];
+    static cudaMemPool_t pools[64];
+    std::call_once(once[dev & 63], [&] {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &props) == cudaSuccess) {
+            uint64_t keep = kPoolKeepBytes;
+            cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+            pools[dev & 63] = p;
+        } else {
+            cudaGetLastError();
+        }
+    });
+    return pools[dev & 63];
+}
+
 // allocating forms: one stream-ordered allocation of buffer + scratch, freed on the stream;
 // the call waits for the sort, as the reference's functions return only when sorted
 static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const void *input, void *output, bool inplace,
@@ -322,7 +362,10 @@ static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const voi
     const Layout L = layout_for(r, count);
     const size_t buf_bytes = (size_t(count) * r.elem_bytes + 255) & ~size_t(255);
     void *mem = nullptr;
-    if (cudaMallocAsync(&mem, L.total + buf_bytes, s) != cudaSuccess || !mem) {
+    cudaMemPool_t pool = sort_pool();
+    const cudaError_t ae = pool ? cudaMallocFromPoolAsync(&mem, L.total + buf_bytes, pool, s)
+                                : cudaMallocAsync(&mem, L.total + buf_bytes, s);
+    if (ae != cudaSuccess || !mem) {
         cudaGetLastError();
         return RSBD8G_ERR_NO_MEMORY;
     }

@@ -22,7 +22,7 @@ namespace rsbd8g {
 
 constexpr int kRadixBits = 8;
 constexpr int kBuckets = 1 << kRadixBits;
-constexpr int kMaxPasses = 8;
+constexpr int kMaxPasses = 16;   // 128-bit keys: 16 digit passes
 
 // device status bits (Control::error)
 enum : uint32_t { kDevTimeout = 1u, kDevFault = 2u };
@@ -99,6 +99,85 @@ __device__ __forceinline__ uint32_t digit_of(U k, int pass) {
     return uint32_t(k >> (pass * kRadixBits)) & (kBuckets - 1);
 }
 
+// ---- wide keys --------------------------------------------------------------------------
+// Two little-endian 64-bit words in 16-byte storage, as the reference's test128 / longdoubletest128
+// (Radixsortbidi8.hpp:1061-1100, :1969-2404).  KeyWide<64>: a 128-bit key (integer, or a float
+// word with the sign in bit 127).  KeyWide<16>: x87 extended precision, 64-bit significand in
+// `lo`, sign and 15-bit exponent in the low 16 bits of `hi` (sign = bit 79 of the key); the upper
+// 48 bits of `hi` are padding: ignored by the ordering, moved with the element.
+template <int HB>
+struct alignas(16) KeyWide {
+    uint64_t lo, hi;
+    static constexpr int kHighBits = HB;
+    static constexpr uint64_t kHighMask = HB == 64 ? ~uint64_t(0) : ((uint64_t(1) << HB) - 1u);
+};
+using KeyU128 = KeyWide<64>;
+using KeyX87 = KeyWide<16>;
+
+template <typename U> struct KeyTraits {
+    static constexpr int kDigits = int(sizeof(U));    // 8-bit digit passes
+    __host__ __device__ static constexpr U fill() { return U(~U(0)); }
+};
+template <int HB> struct KeyTraits<KeyWide<HB>> {
+    static constexpr int kDigits = 8 + HB / 8;
+    __host__ __device__ static constexpr KeyWide<HB> fill() { return KeyWide<HB>{~uint64_t(0), ~uint64_t(0)}; }
+};
+
+// the complement of a filtered key (descending order), within the key's bits
+template <typename U>
+__device__ __forceinline__ U key_not(U k) { return U(~k); }
+template <int HB>
+__device__ __forceinline__ KeyWide<HB> key_not(KeyWide<HB> k) {
+    return KeyWide<HB>{~k.lo, ~k.hi & KeyWide<HB>::kHighMask};
+}
+
+template <int HB>
+__device__ __forceinline__ uint32_t digit_of(KeyWide<HB> k, int pass) {
+    return uint32_t(pass < 8 ? (k.lo >> (pass * kRadixBits)) : (k.hi >> ((pass - 8) * kRadixBits))) & (kBuckets - 1);
+}
+
+// K(b) of the same 8 filter combinations on the (64 + HB)-bit key; the result keeps `hi` within
+// HB bits, so the padding of an x87 key never reaches a digit
+template <int MODE, int HB>
+__device__ __forceinline__ KeyWide<HB> filter_key(KeyWide<HB> b) {
+    using K = KeyWide<HB>;
+    constexpr bool ABS = (MODE & 1) != 0, SIGN = (MODE & 2) != 0, FLTP = (MODE & 4) != 0;
+    constexpr uint64_t hm = K::kHighMask, sb = uint64_t(1) << (HB - 1);
+    uint64_t lo = b.lo, hi = b.hi & hm;
+    const uint64_t s = (hi & sb) ? ~uint64_t(0) : 0u;   // sign mask, both words
+    auto add_s = [&](uint64_t l, uint64_t h) {          // (l, h) + (s, s), two's complement
+        const uint64_t r = l + s;
+        return K{r, (h + s + uint64_t(r < l)) & hm};
+    };
+    auto shl1 = [&](uint64_t l, uint64_t h) { return K{l << 1, ((h << 1) | (l >> 63)) & hm}; };
+    if constexpr (ABS != FLTP) {
+        if constexpr (ABS) {
+            if constexpr (SIGN) {                                            // absolute signed
+                K r = add_s(lo, hi);
+                return K{r.lo ^ s, (r.hi ^ s) & hm};
+            } else {                                                         // tiered absolute signed
+                K r = shl1(lo, hi);
+                return K{r.lo ^ s, (r.hi ^ s) & hm};
+            }
+        } else {
+            const uint64_t mh = hi & ~sb;
+            if constexpr (SIGN) {                                            // floating point, MSB flip
+                K r = add_s(lo, mh);
+                return K{r.lo ^ s, ((r.hi ^ s) & hm) ^ sb};
+            } else {                                                         // inside-out floating point
+                return K{lo ^ s, (mh ^ s) & hm};
+            }
+        }
+    } else if constexpr (ABS) {
+        if constexpr (SIGN) return K{lo, hi & ~sb};                          // absolute floating point
+        K r = shl1(lo, hi);                                                  // tiered abs float: rotl 1, LSB flip
+        return K{(r.lo | (hi >> (HB - 1))) ^ 1u, r.hi};
+    } else {
+        if constexpr (SIGN) return K{lo, hi ^ sb};                           // signed, MSB flip
+        return K{lo, hi};                                                    // unsigned
+    }
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -152,6 +231,22 @@ __device__ __forceinline__ U load_member(const unsigned char *p) {
     for (int i = 0; i < int(sizeof(U)); ++i) v |= U(U(p[i]) << (8 * i));
     return v;
 }
+
+template <int HB>
+__device__ __forceinline__ KeyWide<HB> load_member_wide(const unsigned char *p) {
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) return *reinterpret_cast<const KeyWide<HB> *>(p);
+    KeyWide<HB> v{0, 0};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        v.lo |= uint64_t(p[i]) << (8 * i);
+        v.hi |= uint64_t(p[8 + i]) << (8 * i);
+    }
+    return v;
+}
+template <>
+__device__ __forceinline__ KeyU128 load_member<KeyU128>(const unsigned char *p) { return load_member_wide<64>(p); }
+template <>
+__device__ __forceinline__ KeyX87 load_member<KeyX87>(const unsigned char *p) { return load_member_wide<16>(p); }
 
 __device__ __forceinline__ const unsigned char *load_ptr(const unsigned char *p) {
     if ((reinterpret_cast<uintptr_t>(p) & 7u) == 0) return *reinterpret_cast<const unsigned char *const *>(p);

@@ -14,7 +14,9 @@ namespace rsbd8g {
 struct Resolved {
     Filter f;
     uint32_t rev;         // effective isrevorder
-    uint32_t key_bytes;   // 1, 2, 4, 8
+    uint32_t key_bytes;   // 1, 2, 4, 8, 16
+    uint32_t x87;         // 16-byte x87 extended precision keys (10 digits)
+    uint32_t digits;      // 8-bit digit passes of the key
     uint32_t elem_bytes;  // bytes per array element (key bytes, or 8 for object pointers)
     uint32_t indirect;    // RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2
     uint32_t flags;
@@ -53,13 +55,16 @@ RSBD8G_DECLARE_LAUNCH(launch_sort_k1)
 RSBD8G_DECLARE_LAUNCH(launch_sort_k2)
 RSBD8G_DECLARE_LAUNCH(launch_sort_k4)
 RSBD8G_DECLARE_LAUNCH(launch_sort_k8)
+RSBD8G_DECLARE_LAUNCH(launch_sort_k16)
+RSBD8G_DECLARE_LAUNCH(launch_sort_x87)
 
 // tile geometry of the onesweep passes, per key size (keys per tile = threads * items)
 struct SweepGeometry {
     int threads, items;
 };
 constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
-    return indirect ? SweepGeometry{512, 8} : SweepGeometry{512, key_bytes == 8 ? 16 : 24};
+    if (indirect) return SweepGeometry{512, key_bytes == 16 ? 6 : 8};
+    return SweepGeometry{512, key_bytes == 16 ? 8 : (key_bytes == 8 ? 16 : 24)};
 }
 // the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
 // segment's last tile is partly empty, and large 8-byte segments are the shorter ones)

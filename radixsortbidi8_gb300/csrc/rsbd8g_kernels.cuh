@@ -41,12 +41,16 @@ __device__ __forceinline__ void hist_add(uint32_t *h, uint32_t d, bool valid) {
 template <typename U>
 __device__ __forceinline__ void count_key(uint32_t *sh, U k, bool valid, uint32_t dmask) {
 #pragma unroll
-    for (int p = 0; p < int(sizeof(U)); ++p) hist_add(sh + p * kBuckets, digit_of(k, p) ^ dmask, valid);
+    for (int p = 0; p < KeyTraits<U>::kDigits; ++p) hist_add(sh + p * kBuckets, digit_of(k, p) ^ dmask, valid);
 }
+
+// copies of the gather histogram: fewer for the 16 digits of 128-bit keys (static shared memory)
+template <int P>
+constexpr int gather_hist_copies() { return P > 8 ? 2 : kHistCopies; }
 
 template <int THREADS, int P>
 __device__ __forceinline__ void zero_hist(uint32_t *sh) {
-    for (int i = threadIdx.x; i < kHistCopies * P * kBuckets; i += THREADS) sh[i] = 0;
+    for (int i = threadIdx.x; i < gather_hist_copies<P>() * P * kBuckets; i += THREADS) sh[i] = 0;
     __syncthreads();
 }
 
@@ -56,7 +60,7 @@ __device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long lon
     for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
         uint32_t v = 0;
 #pragma unroll
-        for (int c = 0; c < kHistCopies; ++c) v += sh[c * P * kBuckets + i];
+        for (int c = 0; c < gather_hist_copies<P>(); ++c) v += sh[c * P * kBuckets + i];
         if (v) atomicAdd(ghist + i, (unsigned long long)v);
     }
 }
@@ -67,12 +71,12 @@ __device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long lon
 // 8-byte keys, 128 KB either way).  One 1024-thread CTA per SM reads 16-byte vectors grid-strided;
 // at the end each CTA folds its C copies (rotated reads, conflict-free) into the global histogram.
 template <int P>
-constexpr int hist_lane_copies() { return P <= 4 ? 32 : 16; }
+constexpr int hist_lane_copies() { return P <= 4 ? 32 : (P <= 8 ? 16 : 8); }
 
 template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, uint32_t dmask,
                                                        unsigned long long *__restrict__ ghist) {
-    constexpr int P = int(sizeof(U));
+    constexpr int P = KeyTraits<U>::kDigits;
     constexpr int C = hist_lane_copies<P>();
     constexpr int V = 16 / int(sizeof(U));
     extern __shared__ __align__(16) uint32_t shl[];
@@ -130,10 +134,10 @@ __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__
                                                               const U *__restrict__ keys_in,
                                                               U *__restrict__ keys_out,
                                                               unsigned long long *__restrict__ ghist) {
-    constexpr int P = int(sizeof(U));
-    __shared__ uint32_t shall[kHistCopies * P * kBuckets];
+    constexpr int P = KeyTraits<U>::kDigits;
+    __shared__ uint32_t shall[gather_hist_copies<P>() * P * kBuckets];
     zero_hist<THREADS, P>(shall);
-    uint32_t *sh = shall + ((threadIdx.x >> 5) % kHistCopies) * P * kBuckets;
+    uint32_t *sh = shall + ((threadIdx.x >> 5) % gather_hist_copies<P>()) * P * kBuckets;
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t gwarp = (uint64_t(blockIdx.x) * THREADS + threadIdx.x) >> 5;
     const uint64_t nwarps = (uint64_t(gridDim.x) * THREADS) >> 5;
@@ -143,7 +147,7 @@ __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const uint64_t i = b + u * 32 + lane;
-            raw[u] = 0;
+            raw[u] = U{};
             if (i < n) {
                 if (level == 3) {
                     raw[u] = keys_in[i];
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__
             const uint64_t i = b + u * 32 + lane;
             const bool ok = i < n;
             // the stored key is final: filtered, and complemented for descending sorts
-            const U k = dmask ? U(~filter_key<MODE>(raw[u])) : filter_key<MODE>(raw[u]);
+            const U k = dmask ? key_not(filter_key<MODE>(raw[u])) : filter_key<MODE>(raw[u]);
             if (ok) keys_out[i] = k;
             count_key(sh, k, ok, 0u);
         }
@@ -287,7 +291,7 @@ struct OnesweepSmem {
 // for descending sorts (dmask = 0xFF) -- the descending order is the ascending order of ~K
 template <int MODE, typename U>
 __device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
-    return (uint32_t(filter_key<MODE>(k) >> (pass * kRadixBits)) & (kBuckets - 1)) ^ dmask;
+    return digit_of(filter_key<MODE>(k), pass) ^ dmask;
 }
 
 template <typename U, bool HAS_VAL, int THREADS>
@@ -355,7 +359,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
             const uint64_t gi = tbase + slot;
             const uint64_t si = t.reverse ? (n - 1u - gi) : gi;
             const bool ok = slot < tvalid;
-            keys[i] = ok ? t.src_k[si] : U(~U(0));
+            keys[i] = ok ? t.src_k[si] : KeyTraits<U>::fill();
             if constexpr (HAS_VAL) vals[i] = ok ? t.src_v[si] : 0ull;
         }
     }
@@ -585,7 +589,8 @@ static __global__ void __launch_bounds__(256) k_copy(const Control *__restrict__
         case 1: copy_elems<uint8_t>(c, n); break;
         case 2: copy_elems<uint16_t>(c, n); break;
         case 4: copy_elems<uint32_t>(c, n); break;
-        default: copy_elems<uint64_t>(c, n); break;
+        case 8: copy_elems<uint64_t>(c, n); break;
+        default: copy_elems<uint4>(c, n); break;          // 16-byte elements
     }
 }
 

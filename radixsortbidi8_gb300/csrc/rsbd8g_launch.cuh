@@ -59,7 +59,8 @@ cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, co
             static_cast<const uint64_t *>(in), n, dmask, r.off1, r.off2, int(r.indirect),
             static_cast<const U *>(r.keys), reinterpret_cast<U *>(scratch + L.keys_a), ghist);
     } else {
-        constexpr size_t smem = size_t(hist_lane_copies<int(sizeof(U))>()) * sizeof(U) * kBuckets * 4;
+        constexpr int P = KeyTraits<U>::kDigits;
+        constexpr size_t smem = size_t(hist_lane_copies<P>()) * P * kBuckets * 4;
         auto kern = k_histogram<U, MODE, kHistDirectThreads>;
         static std::once_flag once[64];
         std::call_once(once[dev & 63],
@@ -99,7 +100,7 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     a.to_buffer = to_buffer;
     a.rev = r.rev;
     a.indirect = r.indirect != 0;
-    a.passes = uint32_t(sizeof(U));
+    a.passes = uint32_t(KeyTraits<U>::kDigits);
     const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
     a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
     a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;
@@ -110,7 +111,7 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
                                  reinterpret_cast<unsigned long long *>(scratch + L.bstart), n, a);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const uint32_t P = uint32_t(sizeof(U));
+    const uint32_t P = uint32_t(KeyTraits<U>::kDigits);
     if (r.indirect) {
         e = L.wide_status
                 ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, 0u, s)

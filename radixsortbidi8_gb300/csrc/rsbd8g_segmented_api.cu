@@ -55,7 +55,7 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc,
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
-    if (r.indirect != RSBD8G_DIRECT || !bytes) return RSBD8G_ERR_BAD_ARG;
+    if (r.indirect != RSBD8G_DIRECT || !bytes || r.key_bytes == 16) return RSBD8G_ERR_BAD_ARG;
     SegLayout L;
     if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
     *bytes = L.total;
@@ -69,7 +69,7 @@ static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, siz
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
-    if (r.indirect != RSBD8G_DIRECT) return RSBD8G_ERR_BAD_ARG;
+    if (r.indirect != RSBD8G_DIRECT || r.key_bytes == 16) return RSBD8G_ERR_BAD_ARG;
     if (nsegs == 0 || total == 0) return RSBD8G_OK;
     if (!offsets || !scratch) return RSBD8G_ERR_BAD_ARG;
     if (!in_ptrs) {

@@ -81,3 +81,18 @@ def test_no_cpu_fallback_in_product_path():
     for f in glob.glob(os.path.join(ROOT, "radixsortbidi8_gb300", "**", "*.py"), recursive=True):
         src = open(f).read()
         assert not re.search(r"^\s*(from|import)\s+oracle", src, re.M), f
+
+
+def test_sixteen_byte_key_descriptors():
+    """16-byte keys: 128-bit integer / float words and x87 extended precision; x87 only in 16 bytes."""
+    import radixsortbidi8_gb300 as rs
+    from radixsortbidi8_gb300 import api
+    assert api.key_kind("u128") == (api.KIND_UNSIGNED, 16) and api.key_kind("x87") == (api.KIND_X87, 16)
+    s16 = rs.scratch_bytes("u128", 1 << 20)
+    s10 = rs.scratch_bytes("x87", 1 << 20)
+    assert s16 > s10 > 0               # 16 digit passes of look-back words against 10
+    L = api.lib()
+    out = ctypes.c_size_t(0)
+    for kb, kind in ((8, api.KIND_X87), (2, api.KIND_X87), (12, api.KIND_UNSIGNED), (16, 4)):
+        d = api.Desc(kb, kind, 64, 0, 0, 0, 0, 0)
+        assert L.rsbd8g_scratch_bytes(ctypes.byref(d), 1000, ctypes.byref(out)) == api.ERR_BAD_ARG, (kb, kind)
