@@ -55,7 +55,7 @@ def parse_args():
     p.add_argument("--log2n", type=int, default=28, help="keys per array (2^log2n)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind"],
+    p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind", "u128", "x87"],
                    help="profiling aid: sort only this one array --steps times and print its timings")
     p.add_argument("--config", default="sweep", choices=["sweep", "batched", "serving"],
                    help="sweep: the default line; batched: segmented batches vs a per-array loop; "
@@ -537,7 +537,8 @@ def reference_arm(args, rank: int, world: int) -> dict | None:
 
 def single_case(args) -> dict:
     """One workload alone (for ncu captures of a small case): uniform uint32, int64, the float32
-    absolute descending array, the low-12-bit uint32 array, or the 24-byte record indirection."""
+    absolute descending array, the low-12-bit uint32 array, the 24-byte record indirection, or
+    16-byte keys (128-bit integers ascending, x87 extended precision descending)."""
     import numpy as np
     import torch
     import radixsortbidi8_gb300 as rs
@@ -556,7 +557,10 @@ def single_case(args) -> dict:
         kb, kdt, d, m, gen = {"u32": (4, np.uint32, "ascfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["u32"], n, 4, device=dev)),
                               "i64": (8, np.int64, "ascfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["i64"], n, 8, device=dev)),
                               "f32abs": (4, np.float32, "dscfwdorder", "nativeabs", lambda: S.float_specials_torch(SEEDS["f32"], n, 4, device=dev)),
-                              "u32low12": (4, np.uint32, "ascfwdorder", "native", lambda: S.low_bits_u32_torch(SEEDS["u32low12"], n, device=dev))}[args.case]
+                              "u32low12": (4, np.uint32, "ascfwdorder", "native", lambda: S.low_bits_u32_torch(SEEDS["u32low12"], n, device=dev)),
+                              # 16-byte keys: n keys of two uniform 64-bit words each
+                              "u128": (16, "u128", "ascfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["i64"], 2 * n, 8, device=dev)),
+                              "x87": (16, "x87", "dscfwdorder", "native", lambda: S.uniform_bits_torch(SEEDS["f32"], 2 * n, 8, device=dev))}[args.case]
         bits = gen()
         out, buf = torch.empty_like(bits), torch.empty_like(bits)
         scr = torch.empty(rs.scratch_bytes(kdt, n, d, m), dtype=torch.uint8, device=dev)

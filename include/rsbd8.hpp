@@ -20,6 +20,8 @@
 //                                                         Radixsortbidi8.hpp:2412-2470, :2787-2813
 //   8-bit keys: the single-part noalloc forms without a buffer argument
 //                                                         Radixsortbidi8.hpp:60193-60395
+//   16-byte keys: 128-bit integers and classes (test128), long double (x87 in 16 bytes:
+//   longdoubletest128; binary128 where long double is that)   Radixsortbidi8.hpp:1061-2404, :2849
 // Getters are evaluated on the host for every element (C++ member functions cannot be
 // called from the device), so their objects must be host-accessible; the keys then travel
 // to the device and the pointers are sorted there.  Getters are offered in the allocating
@@ -28,6 +30,7 @@
 
 #include <cuda_runtime_api.h>
 
+#include <cfloat>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -58,15 +61,34 @@ inline rsbd8g_stream &stream_slot() {
     return s;
 }
 
+// 128-bit integers count as integers even where the standard library does not say so
 template <typename T>
-constexpr bool iskeytype{(std::is_arithmetic_v<T> || std::is_enum_v<T> ||
+constexpr bool isint128{
+#ifdef __SIZEOF_INT128__
+    std::is_same_v<std::remove_cv_t<T>, __int128> || std::is_same_v<std::remove_cv_t<T>, unsigned __int128>
+#else
+    false
+#endif
+};
+
+// 16-byte keys: 128-bit integers, 16-byte classes, and long double where it fills 16 bytes
+// (x87 extended precision on x86-64, IEEE binary128 on AArch64)
+template <typename T>
+constexpr bool iskeytype{(std::is_arithmetic_v<T> || std::is_enum_v<T> || isint128<T> ||
                           ((std::is_class_v<T> || std::is_union_v<T>) && std::is_trivially_copyable_v<T>)) &&
-                         (sizeof(T) == 1 || sizeof(T) == 2 || sizeof(T) == 4 || sizeof(T) == 8)};
+                         (sizeof(T) == 1 || sizeof(T) == 2 || sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16)};
 
 template <typename T>
-constexpr uint32_t keykind{std::is_floating_point_v<T> ? uint32_t(RSBD8G_KIND_FLOAT)
-                           : std::is_signed_v<T>        ? uint32_t(RSBD8G_KIND_SIGNED)
-                                                        : uint32_t(RSBD8G_KIND_UNSIGNED)};
+constexpr bool isx87{std::is_same_v<std::remove_cv_t<T>, long double> && LDBL_MANT_DIG == 64 && sizeof(T) == 16};
+
+template <typename T>
+constexpr uint32_t keykind{isx87<T>                                  ? uint32_t(RSBD8G_KIND_X87)
+                           : std::is_floating_point_v<T>               ? uint32_t(RSBD8G_KIND_FLOAT)
+#ifdef __SIZEOF_INT128__
+                           : std::is_same_v<std::remove_cv_t<T>, __int128> ? uint32_t(RSBD8G_KIND_SIGNED)
+#endif
+                           : std::is_signed_v<T>                       ? uint32_t(RSBD8G_KIND_SIGNED)
+                                                                       : uint32_t(RSBD8G_KIND_UNSIGNED)};
 
 template <sortingdirection direction, sortingmode mode, typename T>
 inline rsbd8g_desc makedesc(uint32_t indirection = RSBD8G_DIRECT, std::ptrdiff_t offset1 = 0,

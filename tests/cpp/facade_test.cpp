@@ -4,6 +4,8 @@
 // files (inputs and outputs) for the Python test to compare with the oracle.
 #include <cuda_runtime_api.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -324,6 +326,50 @@ int main(int argc, char **argv) {
         cudaFree(din);
         cudaFree(dout);
         cudaFree(scratch);
+    }
+    {  // 16-byte keys: long double (x87 in 16 bytes on x86-64, binary128 on AArch64) and 128-bit integers
+        const std::size_t n = 5003;
+        std::uint64_t s = 777;
+        std::vector<long double> h(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            const std::int64_t v = std::int64_t(splitmix(s) % 2001) - 1000;     // many ties
+            h[i] = (i % 11 == 0) ? (i % 22 == 0 ? -0.0L : 0.0L) : static_cast<long double>(v) / 7.0L;
+        }
+        long double *din = todev(h), *dout = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dout), n * sizeof(long double));
+        CHECK(rsbd8::radixsortcopy(n, din, dout));
+        std::vector<long double> want = h;
+        std::stable_sort(want.begin(), want.end(), [](long double a, long double b) { return a < b; });
+        const auto got = tohost(dout, n);
+        bool same = true;
+        for (std::size_t i = 0; i < n; ++i)
+            same &= got[i] == want[i] && std::signbit(got[i]) == std::signbit(want[i]);   // -0 and +0 tie, stably
+        CHECK(same);
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::dscfwdorder>(n, din, dout));
+        std::stable_sort(want.begin(), want.end(), [](long double a, long double b) { return b < a; });
+        std::stable_sort(h.begin(), h.end(), [](long double a, long double b) { return b < a; });
+        const auto got2 = tohost(dout, n);
+        same = true;
+        for (std::size_t i = 0; i < n; ++i) same &= got2[i] == h[i] && std::signbit(got2[i]) == std::signbit(h[i]);
+        CHECK(same);
+        cudaFree(din);
+        cudaFree(dout);
+#ifdef __SIZEOF_INT128__
+        std::vector<__int128> q(n);
+        for (auto &x : q) x = (__int128(std::int64_t(splitmix(s))) << 64) | __int128(splitmix(s) % 5);
+        __int128 *dq = todev(q), *dqo = nullptr;
+        cudaMalloc(reinterpret_cast<void **>(&dqo), n * 16);
+        CHECK(rsbd8::radixsortcopy<rsbd8::sortingdirection::dscfwdorder>(n, dq, dqo));
+        std::vector<__int128> qw = q;
+        std::stable_sort(qw.begin(), qw.end(), [](__int128 a, __int128 b) { return b < a; });
+        CHECK(tohost(dqo, n) == qw);
+        CHECK(rsbd8::radixsort(n, reinterpret_cast<unsigned __int128 *>(dq)));
+        std::vector<unsigned __int128> qu(q.begin(), q.end());
+        std::stable_sort(qu.begin(), qu.end());
+        CHECK(tohost(reinterpret_cast<unsigned __int128 *>(dq), n) == qu);
+        cudaFree(dq);
+        cudaFree(dqo);
+#endif
     }
     std::printf("%s (%d failures)\n", failures ? "FAIL" : "PASS", failures);
     return failures ? 1 : 0;
