@@ -295,3 +295,37 @@ def test_indirect_tile_edges(n):
         idx = (out.cpu().numpy() - base) // 24
         want = (O.sortcopy_indirect(host_ptrs, np.float64, 8, "native", d) - np.uint64(rec.ctypes.data)) // 24
         assert np.array_equal(idx, want.astype(np.int64)), d
+
+
+def test_concurrent_calls_from_host_threads():
+    """Calls on disjoint data from several host threads, each on its own stream, are independent
+    (the reference's functions hold no shared mutable state either)."""
+    import threading
+    import torch
+    rs = R()
+    arrays = [mixed_input(dt, 200003 + 17 * i, 40 + i) for i, dt in
+              enumerate([np.uint32, np.float32, np.int64, np.float64, np.uint16, np.int32])]
+    results = [None] * len(arrays)
+    errors = []
+
+    def work(i):
+        try:
+            a = arrays[i]
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                x = to_dev(a)
+                y = empty_dev(a.size, a.dtype)
+                for _ in range(3):
+                    assert rs.radixsortcopy(x, y, "dscrevorder", "native", key_dtype=a.dtype, stream=s)
+                results[i] = from_dev(y, a.dtype)
+        except Exception as e:      # reported below, on the main thread
+            errors.append(e)
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(len(arrays))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for a, got in zip(arrays, results):
+        assert same_bits(got, O.sortcopy(a, "native", "dscrevorder")), a.dtype
