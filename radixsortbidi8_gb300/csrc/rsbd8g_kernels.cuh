@@ -429,7 +429,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
             uint64_t t0 = 0;
             bool done = false;
             while (!done && j >= 0) {
-                constexpr int kWin = 8;
+                constexpr int kWin = sizeof(U) <= 4 ? 4 : 8;   // measured best per key size
                 S w4[kWin];
 #pragma unroll
                 for (int q = 0; q < kWin; ++q)
