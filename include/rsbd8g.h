@@ -88,6 +88,9 @@ enum {
  * the tiles after it run into the bounded device-side wait (200 ms) and the call reports
  * RSBD8G_ERR_TIMEOUT with the output undefined; the device stays usable */
 #define RSBD8G_FLAG_DIAG_STALL 1u
+/* diagnostics only: the allocating forms act as if their device allocation failed (the one
+ * failure the reference reports, as a false return): RSBD8G_ERR_NO_MEMORY, arrays untouched */
+#define RSBD8G_FLAG_DIAG_NOMEM 2u
 
 typedef struct rsbd8g_desc {
     uint32_t key_bytes;     /* 1, 2, 4, 8 or 16 (16: not in the segmented and serving entry points) */

@@ -35,6 +35,7 @@ KIND_UNSIGNED, KIND_SIGNED, KIND_FLOAT, KIND_X87 = 0, 1, 2, 3
 WIDE_KEY_KINDS = {"u128": KIND_UNSIGNED, "i128": KIND_SIGNED, "f128": KIND_FLOAT, "x87": KIND_X87}
 DIRECT, MEMBER, MEMBER2 = 0, 1, 2
 FLAG_DIAG_STALL = 1
+FLAG_DIAG_NOMEM = 2
 
 STATUS = {0: "ok", 1: "bad argument", 2: "device allocation failed", 3: "CUDA runtime error",
           4: "device-side wait timed out", 5: "device-side fault flag", 6: "count too large",

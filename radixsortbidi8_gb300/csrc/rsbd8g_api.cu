@@ -362,6 +362,7 @@ static rsbd8g_status sort_alloc(const rsbd8g_desc *desc, size_t count, const voi
     const Layout L = layout_for(r, count);
     const size_t buf_bytes = (size_t(count) * r.elem_bytes + 255) & ~size_t(255);
     void *mem = nullptr;
+    if (r.flags & RSBD8G_FLAG_DIAG_NOMEM) return RSBD8G_ERR_NO_MEMORY;
     cudaMemPool_t pool = sort_pool();
     const cudaError_t ae = pool ? cudaMallocFromPoolAsync(&mem, L.total + buf_bytes, pool, s)
                                 : cudaMallocAsync(&mem, L.total + buf_bytes, s);

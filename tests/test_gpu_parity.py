@@ -329,3 +329,20 @@ def test_concurrent_calls_from_host_threads():
     assert not errors, errors
     for a, got in zip(arrays, results):
         assert same_bits(got, O.sortcopy(a, "native", "dscrevorder")), a.dtype
+
+
+def test_allocation_failure_returns_false_and_leaves_arrays():
+    """The reference's only failure: the allocation of its scratch fails and radixsort /
+    radixsortcopy return false.  Injected on the host with a diagnostics flag."""
+    import torch
+    from radixsortbidi8_gb300 import api
+    rs = R()
+    a = mixed_input(np.uint32, 10007, 3)
+    x = to_dev(a)
+    y = torch.full_like(x, 7)
+    assert rs.radixsortcopy(x, y, key_dtype=np.uint32, flags=api.FLAG_DIAG_NOMEM) is False
+    assert rs.radixsort(x, key_dtype=np.uint32, flags=api.FLAG_DIAG_NOMEM) is False
+    assert same_bits(from_dev(x, np.uint32), a)
+    assert bool((y == 7).all())
+    assert rs.radixsortcopy(x, y, key_dtype=np.uint32)          # and the next call sorts
+    assert same_bits(from_dev(y, np.uint32), O.sortcopy(a))

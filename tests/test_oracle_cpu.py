@@ -242,3 +242,25 @@ def test_ref_wide_fixture_matches_reference_live():
     a = wide_input("main_x87", 7, 0)
     for d in ("ascfwdorder", "dscfwdorder", "ascrevorder", "dscrevorder"):
         assert np.array_equal(O.ref_sortcopy_wide(a, "x87", "native", d), O.sortcopy_wide(a, "x87", "native", d))
+
+
+def test_oracle_clean_under_address_and_undefined_behaviour_sanitizers(tmp_path):
+    """The C restatement (every key size, mode, direction, both indirection levels, 1-4 threads)
+    built with -fsanitize=address,undefined: no report, and every output ordered and complete."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "oracle_sanitize")
+    r = subprocess.run([gcc, "-std=gnu11", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer",
+                        "-fno-sanitize-recover=all", "-I", os.path.join(root, "oracle"),
+                        os.path.join(root, "oracle", "rsbd8_oracle.c"),
+                        os.path.join(root, "tests", "cpp", "oracle_sanitize.c"), "-o", exe, "-lpthread"],
+                       capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr:
+        pytest.skip("sanitizer runtime not available: " + r.stderr[-200:])
+    assert r.returncode == 0, r.stderr[-2000:]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "PASS" in r.stdout, (r.stdout + r.stderr)[-4000:]
