@@ -364,12 +364,15 @@ def uniform_u32(args, rs, dev, stream, peak) -> dict:
             "histogram_ms": round(sum(hist) / len(hist), 4), "sorted": ok}
 
 
+E2E_SLOTS = 2   # buffer sets of the end-to-end pipeline (three measured slower: 26.8 against 29.7 GKeys/s)
+
+
 def e2e_arm(args, rs, arrays, stream) -> dict:
     """Host buffers in, host buffers out, through the C ABI: every step copies each array's keys
     from pinned host memory, sorts them (radixsortcopynoalloc) and copies the result back.
 
     Pipelined (the headline): one stream per stage -- host-to-device copies, sorts, device-to-host
-    copies -- ordered by events per array, with two sets of device buffers used by alternate steps,
+    copies -- ordered by events per array, with E2E_SLOTS sets of device buffers used in turn by the steps,
     so the copy engines move one array while the SMs sort another.  The NVLink-C2C link to the host
     (about 0.2 TB/s each way, 0.34 TB/s both ways at once) bounds this path.  Serial: the same calls
     one after another on one stream."""
@@ -380,7 +383,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
     n = arrays[0][1].numel()
     h2d = sum(h.numel() * h.element_size() for h in host_in)
     slots = []
-    for _ in range(2):
+    for _ in range(E2E_SLOTS):
         slots.append({
             "in": [torch.empty_like(b) for _, b, *_ in arrays],
             "out": [torch.empty_like(b) for _, b, *_ in arrays],
@@ -392,7 +395,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
     # pipeline: one stream per stage; events order each array's H2D -> sort -> D2H and keep a
     # buffer set from being refilled before the step two back has finished with it
     s_h2d, s_sort, s_d2h = (torch.cuda.Stream(device=dev) for _ in range(3))
-    ev = {key: [[None] * len(arrays) for _ in range(2)] for key in ("h2d", "sort", "d2h")}
+    ev = {key: [[None] * len(arrays) for _ in range(E2E_SLOTS)] for key in ("h2d", "sort", "d2h")}
 
     def record(key, slot_i, i, st):
         e = torch.cuda.Event()
@@ -400,7 +403,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
         ev[key][slot_i][i] = e
 
     def one(k: int, serial: bool):
-        slot_i = k % 2
+        slot_i = k % E2E_SLOTS
         slot = slots[slot_i]
         for i, (nm, b, kdt, d, m) in enumerate(arrays):
             if serial:
@@ -467,12 +470,12 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
 
     copies = {"h2d_alone_GBps": copy_gbps(True, False), "d2h_alone_GBps": copy_gbps(False, True),
               "both_directions_GBps": copy_gbps(True, True)}
-    last = slots[(steps - 1) % 2]
+    last = slots[(steps - 1) % E2E_SLOTS]
     same = all(torch.equal(last["host_out"][i], last["out"][i].cpu()) for i in range(len(arrays)))
     return {"value": round(3 * n / (ms * 1e-3) / 1e9, 3), "unit": "GKeys/s", "ms_per_step": round(ms, 3),
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d, "steps": steps,
             "path": "pinned host -> cudaMemcpyAsync -> radixsortcopynoalloc -> cudaMemcpyAsync -> pinned host; "
-                    "one stream per stage (H2D, sort, D2H) ordered by events, two buffer sets for alternate "
+                    f"one stream per stage (H2D, sort, D2H) ordered by events, {E2E_SLOTS} buffer sets used in turn by the "
                     "steps, so the copy engines move one array while another is sorted",
             "serial": {"value": round(3 * n / (ms_serial * 1e-3) / 1e9, 3), "ms_per_step": round(ms_serial, 3),
                        "path": "the same calls in order on one stream"},
