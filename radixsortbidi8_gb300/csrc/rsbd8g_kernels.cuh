@@ -561,6 +561,263 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
     }
 }
 
+// ---- the pipelined scatter pass (direct keys) -------------------------------------------------
+// Tile B is loaded and ranked while tile A, ranked one iteration earlier and staged in shared
+// memory, waits for its look-back; A's look-back then runs in threads 256..511 while threads 0..255
+// scan B's counts, and A is written out while B's offsets are finished.  The look-back wait of one
+// tile overlaps the load and ranking of the next (four CTA barriers per tile instead of six).
+// Stability and the output are those of k_onesweep: the same slots, ranks and stores, one tile
+// later.  Progress: a CTA's pending tile A only waits on earlier tiles, and ranking B waits on
+// nothing, so the lowest unresolved tile always resolves.
+
+template <typename U, int THREADS, int ITEMS>
+struct PipeSmem {
+    static constexpr int kTile = THREADS * ITEMS;
+    static constexpr int kWarps = THREADS / 32;
+    static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
+    static constexpr size_t kTab = size_t(kWarps) * kBuckets * 4;
+    static constexpr size_t kOffW0 = (kStageK + 15) & ~size_t(15);   // u32 [WARPS][256], table 0
+    static constexpr size_t kOffW1 = kOffW0 + kTab;                   // table 1
+    static constexpr size_t kOffWmask = kOffW1 + kTab;                // u32 [WARPS][256]
+    static constexpr size_t kOffGofs = kOffWmask + kTab;              // i64 [256] of the pending tile
+    static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;     // u64 [256]
+    static constexpr size_t kOffTs = kOffBstart + kBuckets * 8;       // u32 [2][256] tile starts
+    static constexpr size_t kOffCnt = kOffTs + 2 * kBuckets * 4;      // u32 [2][256] tile counts
+    static constexpr size_t kOffMisc = kOffCnt + 2 * kBuckets * 4;    // u32 [32]
+    static constexpr size_t kBytes = kOffMisc + 128;
+};
+
+template <typename U, int MODE, int THREADS, int ITEMS, typename S>
+__global__ void __launch_bounds__(THREADS, 2)
+    k_onesweep_pipe(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
+                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+    static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
+    using L = PipeSmem<U, THREADS, ITEMS>;
+    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
+    constexpr int TILE = L::kTile;
+    constexpr int WARPS = L::kWarps;
+    extern __shared__ __align__(16) unsigned char smem[];
+    U *stage = reinterpret_cast<U *>(smem);
+    uint32_t *wtab0 = reinterpret_cast<uint32_t *>(smem + L::kOffW0);
+    uint32_t *wtab1 = reinterpret_cast<uint32_t *>(smem + L::kOffW1);
+    uint32_t *wmaskall = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
+    uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
+    uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] next tile [1] bad [2..9] scan
+
+    const PassPlan plan = ctrl->plan[pass];
+    if (!plan.active) return;
+    const U *src = static_cast<const U *>(plan.src_keys);
+    U *dst = static_cast<U *>(plan.dst_keys);
+    const bool reverse = plan.reverse != 0;
+    const uint64_t spin_limit = ctrl->spin_limit_ns;
+    const uint32_t stall_tile = ctrl->stall_tile;
+    uint32_t *err_word = &ctrl->error;
+    uint32_t *abort_word = &ctrl->abort;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t ltmask = lanemask_lt();
+
+    for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
+    for (int i = tid; i < WARPS * kBuckets; i += THREADS) {
+        wtab0[i] = 0u;
+        wtab1[i] = 0u;
+        wmaskall[i] = 0u;
+    }
+    if (tid == 0) {
+        misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
+        misc[1] = 0u;
+    }
+    __syncthreads();
+    uint32_t tileB = misc[0];
+    bool hasA = false;
+    uint32_t tileA = 0, tvalidA = 0;
+    int par = 0;                       // table / ts / count parity of tile B
+    for (;;) {
+        const bool hasB = tileB < num_tiles;
+        if (!hasA && !hasB) break;
+        uint32_t *wB = par ? wtab1 : wtab0;
+        uint32_t *wA = par ? wtab0 : wtab1;
+        uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
+        uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
+        uint32_t next = 0xFFFFFFFFu;
+        if (hasB && tid == 0) next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B
+
+        // ---- (1) load and rank tile B: warp-striped slots, warp multisplit as in sweep_tile
+        U keys[ITEMS];
+        uint32_t dr[ITEMS];
+        uint32_t tvalidB = 0;
+        if (hasB) {
+            const uint64_t tbase = uint64_t(tileB) * TILE;
+            tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
+            const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
+            if (!reverse && tvalidB == TILE) {
+                const U *p = src + tbase + slot0;
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+            } else {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) {
+                    const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                    const uint64_t gi = tbase + slot;
+                    keys[i] = slot < tvalidB ? src[reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                dr[i] = slot < tvalidB ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
+            }
+            uint32_t *wcnt = wB + warp * kBuckets;
+            uint32_t *wmask = wmaskall + warp * kBuckets;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t d = dr[i];
+                atomicOr(wmask + d, 1u << lane);
+                __syncwarp();
+                const uint32_t peers = wmask[d];
+                __syncwarp();
+                const uint32_t lower = uint32_t(__popc(peers & ltmask));
+                uint32_t before = 0;
+                if (lower == 0) {
+                    before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
+                    wmask[d] = 0u;
+                }
+                __syncwarp();
+                before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
+                dr[i] = ((before + lower) << 8) | d;
+            }
+        }
+        __syncthreads();                                                        // barrier 1
+
+        // ---- (2a) threads 0..255: B's per-warp offsets and count of digit tid, publish B's aggregate
+        //      (2b) threads 256..511: A's look-back for digit tid - 256, publish A's inclusive prefix
+        uint32_t x = 0, run = 0;
+        if (tid < kBuckets) {
+            if (hasB) {
+#pragma unroll
+                for (int w2 = 0; w2 < WARPS; ++w2) {
+                    const uint32_t c = wB[w2 * kBuckets + tid];
+                    wB[w2 * kBuckets + tid] = run;
+                    run += c;
+                }
+                uint32_t count = run;
+                if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
+                cntB[tid] = count;
+                if (tileB != stall_tile)
+                    st_relaxed(status + size_t(tileB) * kBuckets + tid,
+                               StatusWord<S>::make(tileB == 0 ? kStInclusive : kStAggregate, count));
+                x = run;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) misc[2 + warp] = x;
+            }
+        } else if (hasA) {
+            const int d = tid - kBuckets;
+            const uint32_t count = cntA[d];
+            uint64_t excl = 0;
+            bool bad = false;
+            if (tileA > 0) {
+                int64_t j = int64_t(tileA) - 1;
+                uint32_t spins = 0;
+                uint64_t t0 = 0;
+                bool done = false;
+                while (!done && j >= 0) {
+                    constexpr int kWin = sizeof(U) <= 4 ? 4 : 8;
+                    S w4[kWin];
+#pragma unroll
+                    for (int q = 0; q < kWin; ++q)
+                        w4[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + d) : S(0);
+                    int q = 0;
+                    for (; q < kWin && j - q >= 0; ++q) {
+                        const uint32_t st = StatusWord<S>::state(w4[q]);
+                        if (st == kStInvalid) break;
+                        excl += StatusWord<S>::value(w4[q]);
+                        if (st == kStInclusive) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    if (done) break;
+                    if (q == kWin) {
+                        j -= kWin;
+                        continue;
+                    }
+                    j -= q;
+                    if (++spins > 16u) {
+                        if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
+                        const uint64_t now = globaltimer_ns();
+                        if (t0 == 0) t0 = now;
+                        else if (now - t0 > spin_limit) {
+                            atomicOr(err_word, kDevTimeout);
+                            atomicExch(abort_word, 1u);
+                            bad = true;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+                if (tileA != stall_tile)
+                    st_relaxed(status + size_t(tileA) * kBuckets + d, StatusWord<S>::make(kStInclusive, excl + count));
+            }
+            if (bad) misc[1] = 1u;
+            gofs[d] = (long long)(bstart[d] + excl) - (long long)tsA[d];
+        }
+        __syncthreads();                                                        // barrier 2
+
+        // ---- (3a) threads 0..255: B's tile starts; (3b) all: write A out; clear A's table for the next B
+        if (tid < kBuckets && hasB) {
+            uint32_t before = 0;
+            for (int i = 0; i < warp; ++i) before += misc[2 + i];
+            const uint32_t ts = before + x - run;
+#pragma unroll
+            for (int w2 = 0; w2 < WARPS; ++w2) wB[w2 * kBuckets + tid] += ts;
+            tsB[tid] = ts;
+        }
+        if (hasA && misc[1] == 0u && tileA != stall_tile) {
+            if (tvalidA == TILE) {
+#pragma unroll 4
+                for (int i = 0; i < ITEMS; ++i) {
+                    const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
+                    const U k = stage[s];
+                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    if (uint64_t(g) < n) dst[g] = k;
+                }
+            } else {
+                for (uint32_t s = tid; s < tvalidA; s += THREADS) {
+                    const U k = stage[s];
+                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    if (uint64_t(g) < n) dst[g] = k;
+                }
+            }
+        }
+        for (int i = tid; i < WARPS * kBuckets; i += THREADS) wA[i] = 0u;
+        __syncthreads();                                                        // barrier 3
+
+        // ---- (4) stage B sorted by digit (padding slots land past tvalidB)
+        if (hasB) {
+            const uint32_t *wcnt = wB + warp * kBuckets;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) stage[wcnt[dr[i] & 0xFFu] + (dr[i] >> 8)] = keys[i];
+        }
+        if (tid == 0) {
+            misc[0] = next;
+            misc[1] = 0u;
+        }
+        __syncthreads();                                                        // barrier 4
+        hasA = hasB;
+        tileA = tileB;
+        tvalidA = tvalidB;
+        par ^= 1;
+        tileB = hasB ? misc[0] : num_tiles;
+    }
+}
+
+
 // ---- copy step --------------------------------------------------------------------------------
 
 template <typename T>

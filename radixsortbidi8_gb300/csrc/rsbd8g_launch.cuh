@@ -20,26 +20,42 @@ constexpr int kHistDirectThreads = 1024;  // direct keys: one CTA per SM
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch, uint32_t dmask,
                             cudaStream_t s) {
+    // direct keys: the pipelined pass, unless there are too few tiles to fill its pipeline (a sort
+    // of about one tile per CTA runs each tile's phases back to back in k_onesweep instead)
     using SM = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
+    using PM = PipeSmem<U, THREADS, ITEMS>;
     auto kern = k_onesweep<U, MODE, HAS_VAL, THREADS, ITEMS, S>;
+    auto pkern = k_onesweep_pipe<U, MODE, THREADS, ITEMS, S>;
     int dev = 0;
     cudaGetDevice(&dev);
     static std::once_flag once[64];
-    static int occ[64];
+    static int occ[64], pocc[64];
     std::call_once(once[dev & 63], [&] {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SM::kBytes));
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, THREADS, SM::kBytes);
         occ[dev & 63] = b > 0 ? b : 1;
+        if constexpr (!HAS_VAL) {
+            cudaFuncSetAttribute(pkern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PM::kBytes));
+            cudaFuncSetAttribute(pkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            int pb = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pkern, THREADS, PM::kBytes);
+            pocc[dev & 63] = pb > 0 ? pb : 1;
+        }
     });
-    const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, uint64_t(occ[dev & 63]) * device_sms(dev)));
+    const uint64_t resident = uint64_t(HAS_VAL ? occ[dev & 63] : pocc[dev & 63]) * device_sms(dev);
+    const bool pipe = !HAS_VAL && uint64_t(L.num_tiles) >= 2 * resident;
+    const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, pipe ? resident : uint64_t(occ[dev & 63]) * device_sms(dev)));
     Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
     const unsigned long long *bstart = reinterpret_cast<const unsigned long long *>(scratch + L.bstart);
     for (uint32_t p = 0; p < passes; ++p) {
         S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
         LaunchTimer t(s, RSBD8G_KERNEL_ONESWEEP, uint32_t(sizeof(U)), p, n);
-        kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
+        if (pipe)
+            pkern<<<grid, THREADS, PM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
+        else
+            kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
     }
     return cudaGetLastError();
 }
