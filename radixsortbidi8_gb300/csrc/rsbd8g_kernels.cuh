@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(THREADS, 2)
                 uint64_t t0 = 0;
                 bool done = false;
                 while (!done && j >= 0) {
-                    constexpr int kWin = sizeof(U) <= 4 ? 4 : 8;
+                    constexpr int kWin = sizeof(U) <= 4 ? 4 : (sizeof(U) == 8 ? 2 : 8);   // measured best per key size
                     S w4[kWin];
 #pragma unroll
                     for (int q = 0; q < kWin; ++q)
