@@ -36,20 +36,31 @@ cudaError_t launch_small_t(const SegArgs &a, const U *in, U *out, cudaStream_t s
 template <typename U, int MODE, int THREADS, int ITEMS>
 cudaError_t launch_seg_sweeps_t(const SegArgs &a, const SegLayout &L, unsigned char *scratch, const U *in, U *out,
                                 U *buf, uint32_t stall_tile, cudaStream_t s) {
+    // the pipelined pass when the batch has tiles enough to fill it (tiles_max bounds the large tiles)
     using SM = OnesweepSmem<U, false, THREADS, ITEMS>;
+    using PM = PipeSmem<U, THREADS, ITEMS>;
     auto kern = k_seg_sweep<U, MODE, THREADS, ITEMS>;
+    auto pkern = k_seg_sweep_pipe<U, MODE, THREADS, ITEMS>;
     int dev = 0;
     cudaGetDevice(&dev);
     static std::once_flag once[64];
-    static int occ[64];
+    static int occ[64], pocc[64];
     std::call_once(once[dev & 63], [&] {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SM::kBytes));
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, THREADS, SM::kBytes);
         occ[dev & 63] = b > 0 ? b : 1;
+        cudaFuncSetAttribute(pkern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PM::kBytes));
+        cudaFuncSetAttribute(pkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        int pb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pkern, THREADS, PM::kBytes);
+        pocc[dev & 63] = pb > 0 ? pb : 1;
     });
-    const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(L.tiles_max, uint64_t(occ[dev & 63]) * device_sms(dev))));
+    const uint64_t president = uint64_t(pocc[dev & 63]) * device_sms(dev);
+    const bool pipe = uint64_t(L.tiles_max) >= 2 * president;
+    const uint64_t resident = pipe ? president : uint64_t(occ[dev & 63]) * device_sms(dev);
+    const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(L.tiles_max, resident)));
     uint32_t *status = reinterpret_cast<uint32_t *>(scratch + L.status);
     for (int p = 0; p < int(sizeof(U)); ++p) {
         cudaError_t e;
@@ -59,7 +70,10 @@ cudaError_t launch_seg_sweeps_t(const SegArgs &a, const SegLayout &L, unsigned c
         }
         if (e != cudaSuccess) return e;
         LaunchTimer t(s, RSBD8G_KERNEL_SEGMENTED, uint32_t(sizeof(U)), uint32_t(p), L.tiles_max);
-        kern<<<grid, THREADS, SM::kBytes, s>>>(a, p, int(sizeof(U)), in, out, buf, status, stall_tile);
+        if (pipe)
+            pkern<<<grid, THREADS, PM::kBytes, s>>>(a, p, int(sizeof(U)), in, out, buf, status, stall_tile);
+        else
+            kern<<<grid, THREADS, SM::kBytes, s>>>(a, p, int(sizeof(U)), in, out, buf, status, stall_tile);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

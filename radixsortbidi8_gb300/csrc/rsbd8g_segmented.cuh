@@ -11,6 +11,7 @@
 //   k_seg_plan       per large segment: exclusive scans, pass-skip mask
 //   k_seg_sweep      one onesweep pass over the tiles of every large segment: look-back chains
 //                    stay inside a segment; each segment ping-pongs by its own surviving passes
+//                    (k_seg_sweep_pipe: the same pass with the look-back one tile behind)
 //   k_seg_copy       large segments whose every digit was skipped (plain or reversed copy)
 #pragma once
 #include "rsbd8g_kernels.cuh"
@@ -284,6 +285,262 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
                                                              spin_limit, stall_tile);
         uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
         for (int j = threadIdx.x; j < L::kWarps * kBuckets; j += THREADS) wofs[j] = 0u;
+    }
+}
+
+// One scatter pass over the tiles of every large segment, pipelined as k_onesweep_pipe: tile B is
+// loaded and ranked while tile A (staged in shared memory) waits for its look-back, which threads
+// 256..511 resolve while threads 0..255 scan B's counts.  A tile's segment fixes its source,
+// destination, length, look-back words and bucket starts; a tile whose segment skips this digit is
+// passed over.
+struct SegPipeTile {
+    const void *src;
+    void *dst;
+    const uint32_t *bs;        // bucket starts of this pass for the segment (global)
+    uint32_t *status;          // look-back words of the segment's tile 0
+    uint64_t n;                // keys of the segment
+    uint32_t tile;             // tile index within the segment
+    uint32_t reverse;
+};
+
+template <typename U>
+__device__ __forceinline__ bool seg_pipe_tile(const SegArgs &a, int pass, int passes, const U *in, U *out, U *buf,
+                                              uint32_t *status, uint32_t gt, uint32_t nl, SegPipeTile &t) {
+    const uint32_t idx = seg_of_tile(a.large_tbase, nl, gt);
+    const uint32_t mask = a.seg_mask[idx];
+    if (!((mask >> pass) & 1u)) return false;          // this digit is skipped for the segment
+    const uint32_t seg = a.large_seg[idx];
+    const int k = __popc(mask), i = __popc(mask & ((1u << pass) - 1u)) + 1;
+    U *sin = seg_ptr(a, a.ptr_in, in, seg), *sout = seg_ptr(a, a.ptr_out, out, seg);
+    U *sbuf = seg_ptr(a, a.ptr_buf, buf, seg);
+    t.src = (i == 1) ? sin : (((k - (i - 1)) % 2 == 0) ? sout : sbuf);
+    t.dst = ((k - i) % 2 == 0) ? sout : sbuf;
+    t.bs = a.seg_hist + (size_t(idx) * passes + pass) * kBuckets;
+    t.status = status + size_t(a.large_tbase[idx]) * kBuckets;
+    t.n = seg_len(a.offsets, seg);
+    t.tile = gt - a.large_tbase[idx];
+    t.reverse = (a.rev && i == 1) ? 1u : 0u;
+    return true;
+}
+
+template <typename U, int MODE, int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS, 2)
+    k_seg_sweep_pipe(SegArgs a, int pass, int passes, const U *__restrict__ in, U *__restrict__ out,
+                     U *__restrict__ buf, uint32_t *__restrict__ status, uint32_t stall_tile) {
+    static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
+    using L = PipeSmem<U, THREADS, ITEMS>;
+    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
+    constexpr int TILE = L::kTile;
+    constexpr int WARPS = L::kWarps;
+    extern __shared__ __align__(16) unsigned char smem[];
+    U *stage = reinterpret_cast<U *>(smem);
+    uint32_t *wtab0 = reinterpret_cast<uint32_t *>(smem + L::kOffW0);
+    uint32_t *wtab1 = reinterpret_cast<uint32_t *>(smem + L::kOffW1);
+    uint32_t *wmaskall = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
+    uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] next tile [1] bad [2..9] scan
+    SegControl *c = a.ctrl;
+    if (c->abort) return;
+    const uint32_t T = c->ntiles, nl = c->nlarge;
+    const uint64_t spin_limit = a.spin_limit_ns;
+    uint32_t *err_word = &c->error;
+    uint32_t *abort_word = &c->abort;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t ltmask = lanemask_lt();
+
+    for (int i = tid; i < WARPS * kBuckets; i += THREADS) {
+        wtab0[i] = 0u;
+        wtab1[i] = 0u;
+        wmaskall[i] = 0u;
+    }
+    if (tid == 0) {
+        misc[0] = atomicAdd(&c->tile_counter[pass], 1u);
+        misc[1] = 0u;
+    }
+    __syncthreads();
+    uint32_t gtB = misc[0];
+    bool hasA = false;
+    SegPipeTile A{}, B{};
+    uint32_t tvalidA = 0;
+    int par = 0;
+    for (;;) {
+        const bool claimed = gtB < T;
+        if (!hasA && !claimed) break;
+        const bool hasB = claimed && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, gtB, nl, B);
+        uint32_t *wB = par ? wtab1 : wtab0;
+        uint32_t *wA = par ? wtab0 : wtab1;
+        uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
+        uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
+        uint32_t next = 0xFFFFFFFFu;
+        if (claimed && tid == 0) next = atomicAdd(&c->tile_counter[pass], 1u);
+
+        U keys[ITEMS];
+        uint32_t dr[ITEMS];
+        uint32_t tvalidB = 0;
+        if (hasB) {
+            const U *src = static_cast<const U *>(B.src);
+            const uint64_t n = B.n;
+            const uint64_t tbase = uint64_t(B.tile) * TILE;
+            tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
+            const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
+            if (!B.reverse && tvalidB == TILE) {
+                const U *p = src + tbase + slot0;
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+            } else {
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) {
+                    const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                    const uint64_t gi = tbase + slot;
+                    keys[i] = slot < tvalidB ? src[B.reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                dr[i] = slot < tvalidB ? pass_digit<MODE>(keys[i], pass, a.dmask) : uint32_t(kBuckets - 1);
+            }
+            uint32_t *wcnt = wB + warp * kBuckets;
+            uint32_t *wmask = wmaskall + warp * kBuckets;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t d = dr[i];
+                atomicOr(wmask + d, 1u << lane);
+                __syncwarp();
+                const uint32_t peers = wmask[d];
+                __syncwarp();
+                const uint32_t lower = uint32_t(__popc(peers & ltmask));
+                uint32_t before = 0;
+                if (lower == 0) {
+                    before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
+                    wmask[d] = 0u;
+                }
+                __syncwarp();
+                before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
+                dr[i] = ((before + lower) << 8) | d;
+            }
+        }
+        __syncthreads();                                                        // barrier 1
+
+        uint32_t x = 0, run = 0;
+        if (tid < kBuckets) {
+            if (hasB) {
+#pragma unroll
+                for (int w2 = 0; w2 < WARPS; ++w2) {
+                    const uint32_t cc = wB[w2 * kBuckets + tid];
+                    wB[w2 * kBuckets + tid] = run;
+                    run += cc;
+                }
+                uint32_t count = run;
+                if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
+                cntB[tid] = count;
+                if (B.tile != stall_tile)
+                    st_relaxed(B.status + size_t(B.tile) * kBuckets + tid,
+                               StatusWord<uint32_t>::make(B.tile == 0 ? kStInclusive : kStAggregate, count));
+                x = run;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) misc[2 + warp] = x;
+            }
+        } else if (hasA) {
+            const int d = tid - kBuckets;
+            const uint32_t count = cntA[d];
+            uint64_t excl = 0;
+            bool bad = false;
+            if (A.tile > 0) {
+                int64_t j = int64_t(A.tile) - 1;
+                uint32_t spins = 0;
+                uint64_t t0 = 0;
+                bool done = false;
+                while (!done && j >= 0) {
+                    constexpr int kWin = sizeof(U) <= 4 ? 4 : 2;
+                    uint32_t w4[kWin];
+#pragma unroll
+                    for (int q = 0; q < kWin; ++q)
+                        w4[q] = (j - q >= 0) ? ld_relaxed(A.status + size_t(j - q) * kBuckets + d) : 0u;
+                    int q = 0;
+                    for (; q < kWin && j - q >= 0; ++q) {
+                        const uint32_t st = StatusWord<uint32_t>::state(w4[q]);
+                        if (st == kStInvalid) break;
+                        excl += StatusWord<uint32_t>::value(w4[q]);
+                        if (st == kStInclusive) {
+                            done = true;
+                            break;
+                        }
+                    }
+                    if (done) break;
+                    if (q == kWin) {
+                        j -= kWin;
+                        continue;
+                    }
+                    j -= q;
+                    if (++spins > 16u) {
+                        if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
+                        const uint64_t now = globaltimer_ns();
+                        if (t0 == 0) t0 = now;
+                        else if (now - t0 > spin_limit) {
+                            atomicOr(err_word, kDevTimeout);
+                            atomicExch(abort_word, 1u);
+                            bad = true;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                }
+                if (A.tile != stall_tile)
+                    st_relaxed(A.status + size_t(A.tile) * kBuckets + d,
+                               StatusWord<uint32_t>::make(kStInclusive, excl + count));
+            }
+            if (bad) misc[1] = 1u;
+            gofs[d] = (long long)(uint64_t(A.bs[d]) + excl) - (long long)tsA[d];
+        }
+        __syncthreads();                                                        // barrier 2
+
+        if (tid < kBuckets && hasB) {
+            uint32_t before = 0;
+            for (int i = 0; i < warp; ++i) before += misc[2 + i];
+            const uint32_t ts = before + x - run;
+#pragma unroll
+            for (int w2 = 0; w2 < WARPS; ++w2) wB[w2 * kBuckets + tid] += ts;
+            tsB[tid] = ts;
+        }
+        if (hasA && misc[1] == 0u && A.tile != stall_tile) {
+            U *dst = static_cast<U *>(A.dst);
+            const uint64_t n = A.n;
+            for (uint32_t s = tid; s < tvalidA; s += THREADS) {
+                const U k = stage[s];
+                const long long g = gofs[pass_digit<MODE>(k, pass, a.dmask)] + (long long)s;
+                if (uint64_t(g) < n) dst[g] = k;
+            }
+        }
+        for (int i = tid; i < WARPS * kBuckets; i += THREADS) wA[i] = 0u;
+        __syncthreads();                                                        // barrier 3
+
+        if (hasB) {
+            const uint32_t *wcnt = wB + warp * kBuckets;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) stage[wcnt[dr[i] & 0xFFu] + (dr[i] >> 8)] = keys[i];
+        }
+        if (tid == 0) {
+            misc[0] = next;
+            misc[1] = 0u;
+        }
+        __syncthreads();                                                        // barrier 4
+        // a passed-over tile leaves the pending tile as it was
+        if (hasB) {
+            hasA = true;
+            A = B;
+            tvalidA = tvalidB;
+            par ^= 1;
+        } else {
+            hasA = false;
+        }
+        gtB = claimed ? misc[0] : T;
     }
 }
 
