@@ -346,3 +346,23 @@ def test_allocation_failure_returns_false_and_leaves_arrays():
     assert bool((y == 7).all())
     assert rs.radixsortcopy(x, y, key_dtype=np.uint32)          # and the next call sorts
     assert same_bits(from_dev(y, np.uint32), O.sortcopy(a))
+
+
+def test_lookback_timeout_in_the_pipelined_passes():
+    """The same bounded wait in the pipelined scatter pass (enough tiles to fill its pipeline) and
+    in the pipelined segmented pass: a timeout is reported, nothing hangs, the device keeps working."""
+    import torch
+    from radixsortbidi8_gb300 import api, batched
+    rs = R()
+    a = S.uniform_bits(19, 1 << 23, np.uint32)           # 683 tiles of 12288 keys
+    inp, out = to_dev(a), empty_dev(a.size, np.uint32)
+    with pytest.raises(rs.RSBD8GError) as e:
+        rs.radixsortcopy(inp, out, key_dtype=np.uint32, flags=api.FLAG_DIAG_STALL)
+    assert e.value.status == api.ERR_TIMEOUT
+    offs = torch.arange(0, (1 << 23) + 1, 1 << 20, dtype=torch.int64, device="cuda")   # 8 segments of 2^20
+    nb = batched.segmented_scratch_bytes(np.uint32, a.size, 8)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    buf = empty_dev(a.size, np.uint32)
+    batched.segmented_sortcopy(inp, out, buf, offs, scratch, key_dtype=np.uint32, flags=api.FLAG_DIAG_STALL)
+    assert api.scratch_status(scratch) == api.ERR_TIMEOUT
+    assert same_bits(gpu_copy(a[:100003]), O.sortcopy(a[:100003]))
