@@ -4,6 +4,8 @@ Every case sorts the same seeded input on the GPU and with the oracle's C restat
 (oracle/rsbd8_oracle.c) and compares the bytes: keys, tie order (stability, -0.0/+0.0,
 NaN placement) and, for indirection, the exact pointer order.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -366,3 +368,34 @@ def test_lookback_timeout_in_the_pipelined_passes():
     batched.segmented_sortcopy(inp, out, buf, offs, scratch, key_dtype=np.uint32, flags=api.FLAG_DIAG_STALL)
     assert api.scratch_status(scratch) == api.ERR_TIMEOUT
     assert same_bits(gpu_copy(a[:100003]), O.sortcopy(a[:100003]))
+
+
+# sizes that fill the pipelined scatter pass (at least two tiles per resident CTA on a 152-SM GB300:
+# 683 tiles of 12288 / 6144 / 3072 keys), every key size, filters, directions, in place
+PIPE_CASES = [(np.uint8, 1 << 23, "native", "ascrevorder"), (np.int16, (1 << 23) + 5, "nativeabs", "dscfwdorder"),
+              (np.uint32, (1 << 23) + 7, "native", "dscrevorder"), (np.float32, (1 << 23) + 1, "nativeabs", "dscrevorder"),
+              (np.float32, 1 << 23, "nativetieredabs", "ascrevorder"), (np.int32, 1 << 23, "nativetieredabs", "dscfwdorder"),
+              (np.int64, (1 << 22) + 3, "native", "ascfwdorder"), (np.float64, (1 << 22) + 9, "native", "dscrevorder"),
+              (np.uint64, 1 << 22, 4, "ascrevorder")]
+
+
+@pytest.mark.parametrize("dt,n,mode,direction", PIPE_CASES, ids=lambda v: str(v))
+def test_pipelined_pass_matches_oracle(dt, n, mode, direction):
+    a = mixed_input(dt, n, n % 1000)
+    want = O.sortcopy(a, mode, direction, threads=8)
+    assert same_bits(gpu_copy(a, mode, direction), want)
+    assert same_bits(gpu_inplace(a, mode, direction), want)
+
+
+def test_pipelined_pass_sixteen_byte_keys():
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import torch
+    from make_ref_wide import wide_input
+    rs = R()
+    for kind, gen, mode, d in (("x87", "x87", "native", "dscrevorder"), ("i128", "w128", "native", "ascfwdorder")):
+        a = wide_input(gen, (1 << 21) + 11, 77)
+        x = torch.from_numpy(a.view(np.int64).reshape(-1).copy()).cuda()
+        y = torch.empty_like(x)
+        assert rs.radixsortcopy(x, y, d, mode, key_dtype=kind)
+        assert np.array_equal(y.cpu().numpy().view(np.uint64).reshape(-1, 2), O.sortcopy_wide(a, kind, mode, d)), kind
