@@ -122,3 +122,14 @@ def test_segmented_lookback_timeout_reported():
     from radixsortbidi8_gb300 import api
     assert api.scratch_status(scratch) == api.ERR_TIMEOUT
     _check(a, offs, np.uint32, "native", "ascfwdorder")
+
+
+@pytest.mark.parametrize("dt,mode,direction", [(np.uint32, "native", "dscrevorder"), (np.float64, "nativeabs", "ascrevorder")])
+def test_segmented_pipelined_pass_matches_oracle(dt, mode, direction):
+    """A batch with tiles enough for the pipelined segmented pass (more than two per resident CTA):
+    large segments of uneven sizes, small ones between them, consecutive tiles of one CTA crossing
+    segment boundaries."""
+    rng_lens = [1 << 20, 3, 700001, 0, 5000, (1 << 20) + 77, 12289, 1, 900007, 65536, 2 ** 19 + 5, 44444]
+    lens = rng_lens * 2
+    a, offs = _segments(lens, dt, 31)
+    _check(a, offs, dt, mode, direction)
