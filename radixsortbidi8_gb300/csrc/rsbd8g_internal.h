@@ -64,7 +64,7 @@ struct SweepGeometry {
 };
 constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
     if (indirect) return SweepGeometry{512, key_bytes == 16 ? 6 : 8};
-    return SweepGeometry{512, key_bytes == 16 ? 6 : (key_bytes == 8 ? 12 : 24)};
+    return SweepGeometry{512, key_bytes == 16 ? 6 : (key_bytes == 8 ? 16 : 24)};
 }
 // the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
 // segment's last tile is partly empty, and large 8-byte segments are the shorter ones)

@@ -279,9 +279,8 @@ struct OnesweepSmem {
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
     static constexpr size_t kStageV = HAS_VAL ? size_t(kTile) * 8 : 0;
     static constexpr size_t kOffV = (kStageK + 15) & ~size_t(15);
-    static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32 [WARPS][256]
-    static constexpr size_t kOffWmask = kOffWofs + size_t(kWarps) * kBuckets * 4; // u32 [WARPS][256]
-    static constexpr size_t kOffGofs = kOffWmask + size_t(kWarps) * kBuckets * 4; // i64 [256]
+    static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32 [UNITS][256]
+    static constexpr size_t kOffGofs = kOffWofs + size_t(THREADS / 16) * kBuckets * 4; // i64 [256]
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;              // u64 [256]
     static constexpr size_t kOffMisc = kOffBstart + kBuckets * 8;              // u32 [16]
     static constexpr size_t kBytes = kOffMisc + 64;
@@ -292,6 +291,84 @@ struct OnesweepSmem {
 template <int MODE, typename U>
 __device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
     return digit_of(filter_key<MODE>(k), pass) ^ dmask;
+}
+
+// ---- ranking a tile: the half-warp multisplit ---------------------------------------------------
+// The ranking units of a tile are half-warps: unit u = threadIdx.x / 16 owns the contiguous slots
+// [u * 16 * ITEMS, (u + 1) * 16 * ITEMS), and its item i covers the slots u * 16 * ITEMS + 16 * i +
+// (threadIdx.x mod 16), so ranking in unit, item and lane order ranks in slot order (the sort is
+// stable).  A unit has one shared word per digit: bits 0..15 collect the mask of its lanes that hold
+// the digit in the current item, bits 16..31 keep its running count of the digit.  A lane ORs its
+// bit in (a commutative update: the mask is exact whatever order the lanes run in) and reads the
+// word back -- its rank is the count before the item plus its peers in lower lanes -- and the lowest
+// peer adds the group's size to the count while subtracting the mask, which leaves the mask clear
+// for the next item.  One word carries both, so a key costs three shared-memory operations (an OR,
+// a load, the leaders' add) and no shuffle.  A unit holds at most 16 * ITEMS keys, so counts stay
+// below 2^16; ranks are kept two to a register and the digit is recomputed when the key is staged.
+
+template <int ITEMS>
+__device__ __forceinline__ uint32_t unit_slot0() {
+    return (threadIdx.x >> 4) * 16u * ITEMS + (threadIdx.x & 15u);
+}
+
+template <int MODE, typename U>
+__device__ __forceinline__ uint32_t slot_digit(const U &k, uint32_t slot, uint32_t tvalid, int pass, uint32_t dmask) {
+    return slot < tvalid ? pass_digit<MODE>(k, pass, dmask) : uint32_t(kBuckets - 1);   // padding ranks last
+}
+
+// rank the ITEMS keys of this lane within its unit; urow = the unit's 256 words (masks clear)
+template <int MODE, int ITEMS, typename U>
+__device__ __forceinline__ void rank_unit(const U (&keys)[ITEMS], uint32_t (&rk)[(ITEMS + 1) / 2], uint32_t *urow,
+                                          uint32_t slot0, uint32_t tvalid, int pass, uint32_t dmask) {
+    const uint32_t hbit = 1u << (threadIdx.x & 15u), below = hbit - 1u;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalid, pass, dmask);
+        atomicOr(urow + d, hbit);
+        __syncwarp();
+        const uint32_t w = urow[d];
+        __syncwarp();
+        const uint32_t peers = w & 0xFFFFu;
+        const uint32_t lower = uint32_t(__popc(peers & below));
+        if (lower == 0) atomicAdd(urow + d, (uint32_t(__popc(peers)) << 16) - peers);
+        __syncwarp();          // the cleared mask is visible to the next item's updates
+        const uint32_t r = (w >> 16) + lower;
+        if (i & 1) rk[i >> 1] |= r << 16;
+        else rk[i >> 1] = r;
+    }
+}
+
+template <int ITEMS>
+__device__ __forceinline__ uint32_t unit_rank(const uint32_t (&rk)[(ITEMS + 1) / 2], int i) {
+    return (rk[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+}
+
+// digit d's count in the tile: the sum over the units (after ranking a word holds count << 16)
+template <int UNITS>
+__device__ __forceinline__ uint32_t units_total(const uint32_t *tab, int d) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int u = 0; u < UNITS; ++u) run += tab[u * kBuckets + d] >> 16;
+    return run;
+}
+
+// replace digit d's unit counts by the units' staging offsets, the first one at the tile start ts
+template <int UNITS>
+__device__ __forceinline__ void units_offsets(uint32_t *tab, int d, uint32_t ts) {
+#pragma unroll
+    for (int u = 0; u < UNITS; ++u) {
+        const uint32_t c = tab[u * kBuckets + d] >> 16;
+        tab[u * kBuckets + d] = ts;
+        ts += c;
+    }
+}
+
+// a warp clears the words of its two units once its keys are staged, ready for the next tile
+__device__ __forceinline__ void clear_warp_units(uint32_t *tab) {
+    uint32_t *rows = tab + (threadIdx.x >> 5) * 2u * kBuckets;
+    __syncwarp();
+#pragma unroll
+    for (int i = threadIdx.x & 31; i < 2 * kBuckets; i += 32) rows[i] = 0u;
 }
 
 template <typename U, bool HAS_VAL, int THREADS>
@@ -312,7 +389,7 @@ struct SweepTile {
     bool reverse;             // read the source back to front
 };
 
-// Process one tile: load, rank (warp multisplit), publish and resolve the look-back, stage sorted
+// Process one tile: load, rank (half-warp multisplit), publish and resolve the look-back, stage sorted
 // by digit in shared memory, write out.  `bstart` (shared) holds the bucket starts of this pass for
 // the array / segment.  Called by all threads; ends with a barrier.
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
@@ -322,40 +399,38 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
                                            uint32_t stall_tile) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     constexpr int TILE = L::kTile;
-    constexpr int WARPS = L::kWarps;
+    constexpr int UNITS = THREADS / 16;
     U *stage_k = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..17] scan
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t *wcnt = wofs + warp * kBuckets;
-    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask) + warp * kBuckets;
-    const uint32_t ltmask = lanemask_lt();
+    uint32_t *urow = wofs + (uint32_t(tid) >> 4) * kBuckets;
     const uint32_t tile = t.tile;
     const uint64_t n = t.n;
     const uint64_t tbase = uint64_t(tile) * TILE;
     const uint32_t tvalid = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
 
-    // load ITEMS keys per thread, warp-striped: item i of lane l is slot w*32*ITEMS + i*32 + l.
+    // load ITEMS keys per thread: item i of this lane is slot unit_slot0 + 16 i (see rank_unit).
     // Slots past the end get digit 255: they rank after every real key of the tile.
     U keys[ITEMS];
     uint64_t vals[HAS_VAL ? ITEMS : 1];
-    uint32_t dr[ITEMS];      // digit, later (rank << 8) | digit
-    const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
+    uint32_t rk[(ITEMS + 1) / 2];
+    const uint32_t slot0 = unit_slot0<ITEMS>();
     if (!t.reverse && tvalid == TILE) {
         const U *p = t.src_k + tbase + slot0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
         if constexpr (HAS_VAL) {
             const uint64_t *q = t.src_v + tbase + slot0;
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 32];
+            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 16];
         }
     } else {
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t slot = slot0 + uint32_t(i) * 32u;
+            const uint32_t slot = slot0 + uint32_t(i) * 16u;
             const uint64_t gi = tbase + slot;
             const uint64_t si = t.reverse ? (n - 1u - gi) : gi;
             const bool ok = slot < tvalid;
@@ -363,43 +438,13 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
             if constexpr (HAS_VAL) vals[i] = ok ? t.src_v[si] : 0ull;
         }
     }
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t slot = slot0 + uint32_t(i) * 32u;
-        dr[i] = slot < tvalid ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
-    }
-    // warp multisplit in slot order: the lanes holding digit d OR their bit into the warp's mask
-    // word for d (a commutative update, so the mask is exact whatever order the lanes run in) and
-    // read it back; the lowest lane of the group advances the warp's running count of d with one
-    // returning atomic, clears the mask for the next item, and hands the old count to its peers
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = dr[i];
-        atomicOr(wmask + d, 1u << lane);
-        __syncwarp();
-        const uint32_t peers = wmask[d];
-        __syncwarp();
-        const uint32_t lower = uint32_t(__popc(peers & ltmask));
-        uint32_t before = 0;
-        if (lower == 0) {
-            before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
-            wmask[d] = 0u;
-        }
-        __syncwarp();          // the cleared masks are visible to the next item's updates
-        before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
-        dr[i] = ((before + lower) << 8) | d;
-    }
+    rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalid, pass, dmask);
     __syncthreads();
 
-    // per digit: exclusive offsets of the warps and the tile count; publish the aggregate
+    // per digit: the tile count; publish the aggregate
     uint32_t count = 0, x = 0, run = 0;
     if (tid < kBuckets) {
-#pragma unroll
-        for (int w2 = 0; w2 < WARPS; ++w2) {
-            const uint32_t c = wofs[w2 * kBuckets + tid];
-            wofs[w2 * kBuckets + tid] = run;
-            run += c;
-        }
+        run = units_total<UNITS>(wofs, tid);
         count = run;
         if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalid;   // the padding slots
         if (tile != stall_tile)
@@ -418,9 +463,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
         uint32_t before = 0;
         for (int i = 0; i < warp; ++i) before += misc[2 + i];
         const uint32_t ts = before + x - run;          // tile start of digit tid
-#pragma unroll
-        for (int w2 = 0; w2 < WARPS; ++w2) wofs[w2 * kBuckets + tid] += ts;
-        // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
+        units_offsets<UNITS>(wofs, tid, ts);
+    // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
         uint64_t excl = 0;
         bool bad = false;
         if (tile > 0) {
@@ -476,10 +520,12 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     // stage the tile in shared memory, sorted by digit (padding slots land past tvalid)
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t pos = wcnt[dr[i] & 0xFFu] + (dr[i] >> 8);
+        const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalid, pass, dmask);
+        const uint32_t pos = urow[d] + unit_rank<ITEMS>(rk, i);
         stage_k[pos] = keys[i];
         if constexpr (HAS_VAL) stage_v[pos] = vals[i];
     }
+    clear_warp_units(wofs);
     __syncthreads();
     // write out: consecutive threads take consecutive slots of a bucket run
     if (!tile_bad) {
@@ -511,12 +557,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __device__ __forceinline__ void sweep_init_smem(unsigned char *smem) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
-    uint32_t *wmask = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
     uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
-    for (int i = threadIdx.x; i < L::kWarps * kBuckets; i += THREADS) {
-        wmask[i] = 0u;
-        wofs[i] = 0u;
-    }
+    for (int i = threadIdx.x; i < (THREADS / 16) * kBuckets; i += THREADS) wofs[i] = 0u;
 }
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
@@ -555,9 +597,6 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
         t.tile = tile;
         sweep_tile<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem, t, bstart, pass, dmask, &ctrl->error, &ctrl->abort,
                                                         spin_limit, stall_tile);
-        // sweep_tile leaves the warp counters holding offsets: zero them for the next tile
-        uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
-        for (int i = threadIdx.x; i < L::kWarps * kBuckets; i += THREADS) wofs[i] = 0u;
     }
 }
 
@@ -568,18 +607,17 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
 // tile overlaps the load and ranking of the next (four CTA barriers per tile instead of six).
 // Stability and the output are those of k_onesweep: the same slots, ranks and stores, one tile
 // later.  Progress: a CTA's pending tile A only waits on earlier tiles, and ranking B waits on
-// nothing, so the lowest unresolved tile always resolves.
+// nothing, so the lowest unresolved tile always resolves.  Tile B's unit words are scanned into
+// offsets in (3a) and cleared by each warp once B is staged in (4), so one table serves every tile.
 
 template <typename U, int THREADS, int ITEMS>
 struct PipeSmem {
     static constexpr int kTile = THREADS * ITEMS;
     static constexpr int kWarps = THREADS / 32;
+    static constexpr int kUnits = THREADS / 16;
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
-    static constexpr size_t kTab = size_t(kWarps) * kBuckets * 4;
-    static constexpr size_t kOffW0 = (kStageK + 15) & ~size_t(15);   // u32 [WARPS][256], table 0
-    static constexpr size_t kOffW1 = kOffW0 + kTab;                   // table 1
-    static constexpr size_t kOffWmask = kOffW1 + kTab;                // u32 [WARPS][256]
-    static constexpr size_t kOffGofs = kOffWmask + kTab;              // i64 [256] of the pending tile
+    static constexpr size_t kOffUnits = (kStageK + 15) & ~size_t(15);  // u32 [UNITS][256]
+    static constexpr size_t kOffGofs = kOffUnits + size_t(kUnits) * kBuckets * 4;   // i64 [256] of tile A
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;     // u64 [256]
     static constexpr size_t kOffTs = kOffBstart + kBuckets * 8;       // u32 [2][256] tile starts
     static constexpr size_t kOffCnt = kOffTs + 2 * kBuckets * 4;      // u32 [2][256] tile counts
@@ -595,12 +633,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     using L = PipeSmem<U, THREADS, ITEMS>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
-    constexpr int WARPS = L::kWarps;
+    constexpr int UNITS = L::kUnits;
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
-    uint32_t *wtab0 = reinterpret_cast<uint32_t *>(smem + L::kOffW0);
-    uint32_t *wtab1 = reinterpret_cast<uint32_t *>(smem + L::kOffW1);
-    uint32_t *wmaskall = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
     uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
@@ -617,14 +653,11 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t *err_word = &ctrl->error;
     uint32_t *abort_word = &ctrl->abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t ltmask = lanemask_lt();
+    uint32_t *urow = utab + (uint32_t(tid) >> 4) * kBuckets;
+    const uint32_t slot0 = unit_slot0<ITEMS>();
 
     for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
-    for (int i = tid; i < WARPS * kBuckets; i += THREADS) {
-        wtab0[i] = 0u;
-        wtab1[i] = 0u;
-        wmaskall[i] = 0u;
-    }
+    for (int i = tid; i < UNITS * kBuckets; i += THREADS) utab[i] = 0u;
     if (tid == 0) {
         misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
         misc[1] = 0u;
@@ -633,75 +666,44 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t tileB = misc[0];
     bool hasA = false;
     uint32_t tileA = 0, tvalidA = 0;
-    int par = 0;                       // table / ts / count parity of tile B
+    int par = 0;                       // ts / count parity of tile B
     for (;;) {
         const bool hasB = tileB < num_tiles;
         if (!hasA && !hasB) break;
-        uint32_t *wB = par ? wtab1 : wtab0;
-        uint32_t *wA = par ? wtab0 : wtab1;
         uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
         uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
         uint32_t next = 0xFFFFFFFFu;
         if (hasB && tid == 0) next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B
 
-        // ---- (1) load and rank tile B: warp-striped slots, warp multisplit as in sweep_tile
+        // ---- (1) load and rank tile B (half-warp units, as in sweep_tile)
         U keys[ITEMS];
-        uint32_t dr[ITEMS];
+        uint32_t rk[(ITEMS + 1) / 2];
         uint32_t tvalidB = 0;
         if (hasB) {
             const uint64_t tbase = uint64_t(tileB) * TILE;
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
-            const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
             if (!reverse && tvalidB == TILE) {
                 const U *p = src + tbase + slot0;
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
             } else {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                    const uint32_t slot = slot0 + uint32_t(i) * 16u;
                     const uint64_t gi = tbase + slot;
                     keys[i] = slot < tvalidB ? src[reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
                 }
             }
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t slot = slot0 + uint32_t(i) * 32u;
-                dr[i] = slot < tvalidB ? pass_digit<MODE>(keys[i], pass, dmask) : uint32_t(kBuckets - 1);
-            }
-            uint32_t *wcnt = wB + warp * kBuckets;
-            uint32_t *wmask = wmaskall + warp * kBuckets;
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t d = dr[i];
-                atomicOr(wmask + d, 1u << lane);
-                __syncwarp();
-                const uint32_t peers = wmask[d];
-                __syncwarp();
-                const uint32_t lower = uint32_t(__popc(peers & ltmask));
-                uint32_t before = 0;
-                if (lower == 0) {
-                    before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
-                    wmask[d] = 0u;
-                }
-                __syncwarp();
-                before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
-                dr[i] = ((before + lower) << 8) | d;
-            }
+            rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalidB, pass, dmask);
         }
         __syncthreads();                                                        // barrier 1
 
-        // ---- (2a) threads 0..255: B's per-warp offsets and count of digit tid, publish B's aggregate
+        // ---- (2a) threads 0..255: B's count of digit tid, publish B's aggregate
         //      (2b) threads 256..511: A's look-back for digit tid - 256, publish A's inclusive prefix
         uint32_t x = 0, run = 0;
         if (tid < kBuckets) {
             if (hasB) {
-#pragma unroll
-                for (int w2 = 0; w2 < WARPS; ++w2) {
-                    const uint32_t c = wB[w2 * kBuckets + tid];
-                    wB[w2 * kBuckets + tid] = run;
-                    run += c;
-                }
+                run = units_total<UNITS>(utab, tid);
                 uint32_t count = run;
                 if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
                 cntB[tid] = count;
@@ -769,13 +771,12 @@ __global__ void __launch_bounds__(THREADS, 2)
         }
         __syncthreads();                                                        // barrier 2
 
-        // ---- (3a) threads 0..255: B's tile starts; (3b) all: write A out; clear A's table for the next B
+        // ---- (3a) threads 0..255: B's tile starts and unit offsets; (3b) all: write A out
         if (tid < kBuckets && hasB) {
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
             const uint32_t ts = before + x - run;
-#pragma unroll
-            for (int w2 = 0; w2 < WARPS; ++w2) wB[w2 * kBuckets + tid] += ts;
+            units_offsets<UNITS>(utab, tid, ts);
             tsB[tid] = ts;
         }
         if (hasA && misc[1] == 0u && tileA != stall_tile) {
@@ -795,14 +796,16 @@ __global__ void __launch_bounds__(THREADS, 2)
                 }
             }
         }
-        for (int i = tid; i < WARPS * kBuckets; i += THREADS) wA[i] = 0u;
         __syncthreads();                                                        // barrier 3
 
-        // ---- (4) stage B sorted by digit (padding slots land past tvalidB)
+        // ---- (4) stage B sorted by digit (padding slots land past tvalidB); clear the unit words
         if (hasB) {
-            const uint32_t *wcnt = wB + warp * kBuckets;
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) stage[wcnt[dr[i] & 0xFFu] + (dr[i] >> 8)] = keys[i];
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalidB, pass, dmask);
+                stage[urow[d] + unit_rank<ITEMS>(rk, i)] = keys[i];
+            }
+            clear_warp_units(utab);
         }
         if (tid == 0) {
             misc[0] = next;

@@ -283,8 +283,6 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
         t.reverse = a.rev && i == 1;
         sweep_tile<U, MODE, false, THREADS, ITEMS, uint32_t>(smem, t, bstart, pass, a.dmask, &c->error, &c->abort,
                                                              spin_limit, stall_tile);
-        uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
-        for (int j = threadIdx.x; j < L::kWarps * kBuckets; j += THREADS) wofs[j] = 0u;
     }
 }
 
@@ -331,12 +329,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     using L = PipeSmem<U, THREADS, ITEMS>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
-    constexpr int WARPS = L::kWarps;
+    constexpr int UNITS = L::kUnits;
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
-    uint32_t *wtab0 = reinterpret_cast<uint32_t *>(smem + L::kOffW0);
-    uint32_t *wtab1 = reinterpret_cast<uint32_t *>(smem + L::kOffW1);
-    uint32_t *wmaskall = reinterpret_cast<uint32_t *>(smem + L::kOffWmask);
+    uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
     uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
@@ -348,13 +344,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t *err_word = &c->error;
     uint32_t *abort_word = &c->abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t ltmask = lanemask_lt();
+    uint32_t *urow = utab + (uint32_t(tid) >> 4) * kBuckets;
+    const uint32_t slot0 = unit_slot0<ITEMS>();
 
-    for (int i = tid; i < WARPS * kBuckets; i += THREADS) {
-        wtab0[i] = 0u;
-        wtab1[i] = 0u;
-        wmaskall[i] = 0u;
-    }
+    for (int i = tid; i < UNITS * kBuckets; i += THREADS) utab[i] = 0u;
     if (tid == 0) {
         misc[0] = atomicAdd(&c->tile_counter[pass], 1u);
         misc[1] = 0u;
@@ -369,70 +362,39 @@ __global__ void __launch_bounds__(THREADS, 2)
         const bool claimed = gtB < T;
         if (!hasA && !claimed) break;
         const bool hasB = claimed && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, gtB, nl, B);
-        uint32_t *wB = par ? wtab1 : wtab0;
-        uint32_t *wA = par ? wtab0 : wtab1;
         uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
         uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
         uint32_t next = 0xFFFFFFFFu;
         if (claimed && tid == 0) next = atomicAdd(&c->tile_counter[pass], 1u);
 
         U keys[ITEMS];
-        uint32_t dr[ITEMS];
+        uint32_t rk[(ITEMS + 1) / 2];
         uint32_t tvalidB = 0;
         if (hasB) {
             const U *src = static_cast<const U *>(B.src);
             const uint64_t n = B.n;
             const uint64_t tbase = uint64_t(B.tile) * TILE;
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
-            const uint32_t slot0 = uint32_t(warp) * 32u * ITEMS + uint32_t(lane);
             if (!B.reverse && tvalidB == TILE) {
                 const U *p = src + tbase + slot0;
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 32];
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
             } else {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * 32u;
+                    const uint32_t slot = slot0 + uint32_t(i) * 16u;
                     const uint64_t gi = tbase + slot;
                     keys[i] = slot < tvalidB ? src[B.reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
                 }
             }
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t slot = slot0 + uint32_t(i) * 32u;
-                dr[i] = slot < tvalidB ? pass_digit<MODE>(keys[i], pass, a.dmask) : uint32_t(kBuckets - 1);
-            }
-            uint32_t *wcnt = wB + warp * kBuckets;
-            uint32_t *wmask = wmaskall + warp * kBuckets;
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t d = dr[i];
-                atomicOr(wmask + d, 1u << lane);
-                __syncwarp();
-                const uint32_t peers = wmask[d];
-                __syncwarp();
-                const uint32_t lower = uint32_t(__popc(peers & ltmask));
-                uint32_t before = 0;
-                if (lower == 0) {
-                    before = atomicAdd(wcnt + d, uint32_t(__popc(peers)));
-                    wmask[d] = 0u;
-                }
-                __syncwarp();
-                before = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1);
-                dr[i] = ((before + lower) << 8) | d;
-            }
+            rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalidB, pass, a.dmask);
         }
         __syncthreads();                                                        // barrier 1
 
         uint32_t x = 0, run = 0;
         if (tid < kBuckets) {
             if (hasB) {
-#pragma unroll
-                for (int w2 = 0; w2 < WARPS; ++w2) {
-                    const uint32_t cc = wB[w2 * kBuckets + tid];
-                    wB[w2 * kBuckets + tid] = run;
-                    run += cc;
-                }
+                run = units_total<UNITS>(utab, tid);
                 uint32_t count = run;
                 if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
                 cntB[tid] = count;
@@ -505,8 +467,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
             const uint32_t ts = before + x - run;
-#pragma unroll
-            for (int w2 = 0; w2 < WARPS; ++w2) wB[w2 * kBuckets + tid] += ts;
+            units_offsets<UNITS>(utab, tid, ts);
             tsB[tid] = ts;
         }
         if (hasA && misc[1] == 0u && A.tile != stall_tile) {
@@ -518,13 +479,15 @@ __global__ void __launch_bounds__(THREADS, 2)
                 if (uint64_t(g) < n) dst[g] = k;
             }
         }
-        for (int i = tid; i < WARPS * kBuckets; i += THREADS) wA[i] = 0u;
         __syncthreads();                                                        // barrier 3
 
         if (hasB) {
-            const uint32_t *wcnt = wB + warp * kBuckets;
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) stage[wcnt[dr[i] & 0xFFu] + (dr[i] >> 8)] = keys[i];
+            for (int i = 0; i < ITEMS; ++i) {
+                const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalidB, pass, a.dmask);
+                stage[urow[d] + unit_rank<ITEMS>(rk, i)] = keys[i];
+            }
+            clear_warp_units(utab);
         }
         if (tid == 0) {
             misc[0] = next;
