@@ -94,7 +94,7 @@ constexpr int kSegSmallVariants = 3;
 
 // byte offsets of the parts of a segmented-sort scratch area
 struct SegLayout {
-    size_t ctrl, large_seg, large_tbase, small_seg, seg_hist, seg_mask, status, status_bytes, zero_bytes, total;
+    size_t ctrl, large_seg, large_tbase, small_seg, seg_hist, seg_mask, tile_seg, status, status_bytes, zero_bytes, total;
     uint64_t nlarge_max, tiles_max;
     uint32_t cutoff, small_variant, tile;
 };

@@ -279,7 +279,7 @@ struct OnesweepSmem {
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
     static constexpr size_t kStageV = HAS_VAL ? size_t(kTile) * 8 : 0;
     static constexpr size_t kOffV = (kStageK + 15) & ~size_t(15);
-    static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32 [UNITS][256]
+    static constexpr size_t kOffWofs = kOffV + kStageV;                       // u32: the TileRank table
     static constexpr size_t kOffGofs = kOffWofs + size_t(THREADS / 16) * kBuckets * 4; // i64 [256]
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;              // u64 [256]
     static constexpr size_t kOffMisc = kOffBstart + kBuckets * 8;              // u32 [16]
@@ -293,82 +293,199 @@ __device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
     return digit_of(filter_key<MODE>(k), pass) ^ dmask;
 }
 
-// ---- ranking a tile: the half-warp multisplit ---------------------------------------------------
-// The ranking units of a tile are half-warps: unit u = threadIdx.x / 16 owns the contiguous slots
-// [u * 16 * ITEMS, (u + 1) * 16 * ITEMS), and its item i covers the slots u * 16 * ITEMS + 16 * i +
-// (threadIdx.x mod 16), so ranking in unit, item and lane order ranks in slot order (the sort is
-// stable).  A unit has one shared word per digit: bits 0..15 collect the mask of its lanes that hold
-// the digit in the current item, bits 16..31 keep its running count of the digit.  A lane ORs its
-// bit in (a commutative update: the mask is exact whatever order the lanes run in) and reads the
-// word back -- its rank is the count before the item plus its peers in lower lanes -- and the lowest
-// peer adds the group's size to the count while subtracting the mask, which leaves the mask clear
-// for the next item.  One word carries both, so a key costs three shared-memory operations (an OR,
-// a load, the leaders' add) and no shuffle.  A unit holds at most 16 * ITEMS keys, so counts stay
-// below 2^16; ranks are kept two to a register and the digit is recomputed when the key is staged.
-
-template <int ITEMS>
-__device__ __forceinline__ uint32_t unit_slot0() {
-    return (threadIdx.x >> 4) * 16u * ITEMS + (threadIdx.x & 15u);
-}
+// ---- ranking a tile: the warp multisplit ----------------------------------------------------------
+// A tile is ranked in units of LANES lanes (a half-warp or a warp): unit u = threadIdx.x / LANES owns
+// the contiguous slots [u * LANES * ITEMS, (u + 1) * LANES * ITEMS), and its item i covers the slots
+// u * LANES * ITEMS + LANES * i + (threadIdx.x mod LANES), so ranking in unit, item and lane order
+// ranks in slot order (the sort is stable).  The lanes of a unit holding digit d in an item OR their
+// bit into a mask word for d (a commutative update: the mask is exact whatever order the lanes run
+// in) and read it back; a lane's rank is the unit's count of d before the item plus its peers in
+// lower lanes, and the lowest peer advances the count and clears the mask for the next item.
+//   Half-warp units (LANES 16) keep mask and count in one word per (unit, digit): bits 0..15 the
+// mask, bits 16..31 the count.  The word read back carries the count too, and the leader's single
+// add of (group size << 16) - mask advances the count and clears the mask: three shared-memory
+// operations per key and no shuffle.
+//   Warp units (LANES 32) keep a count word per (warp, digit) and a mask word per (warp, digit); the
+// leader advances the count with one returning atomic, clears the mask and hands the old count to
+// its peers with a shuffle: four operations and a shuffle per key, but half as many units to scan
+// per tile, which pays for small tiles.
+// Both tables take (THREADS / 16) * 256 words.  A unit holds at most LANES * ITEMS keys, so counts
+// stay below 2^16.  Large tiles keep their ranks two to a register and recompute the digit when the
+// key is staged (registers are what limits them); small tiles keep (rank << 8) | digit per key.
 
 template <int MODE, typename U>
 __device__ __forceinline__ uint32_t slot_digit(const U &k, uint32_t slot, uint32_t tvalid, int pass, uint32_t dmask) {
     return slot < tvalid ? pass_digit<MODE>(k, pass, dmask) : uint32_t(kBuckets - 1);   // padding ranks last
 }
 
-// rank the ITEMS keys of this lane within its unit; urow = the unit's 256 words (masks clear)
-template <int MODE, int ITEMS, typename U>
-__device__ __forceinline__ void rank_unit(const U (&keys)[ITEMS], uint32_t (&rk)[(ITEMS + 1) / 2], uint32_t *urow,
-                                          uint32_t slot0, uint32_t tvalid, int pass, uint32_t dmask) {
-    const uint32_t hbit = 1u << (threadIdx.x & 15u), below = hbit - 1u;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalid, pass, dmask);
-        atomicOr(urow + d, hbit);
-        __syncwarp();
-        const uint32_t w = urow[d];
-        __syncwarp();
-        const uint32_t peers = w & 0xFFFFu;
-        const uint32_t lower = uint32_t(__popc(peers & below));
-        if (lower == 0) atomicAdd(urow + d, (uint32_t(__popc(peers)) << 16) - peers);
-        __syncwarp();          // the cleared mask is visible to the next item's updates
-        const uint32_t r = (w >> 16) + lower;
-        if (i & 1) rk[i >> 1] |= r << 16;
-        else rk[i >> 1] = r;
-    }
-}
-
+// the unit size that measured faster for a tile of THREADS * ITEMS keys
 template <int ITEMS>
-__device__ __forceinline__ uint32_t unit_rank(const uint32_t (&rk)[(ITEMS + 1) / 2], int i) {
-    return (rk[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
-}
+constexpr int rank_lanes() { return ITEMS >= 16 ? 16 : 32; }
 
-// digit d's count in the tile: the sum over the units (after ranking a word holds count << 16)
-template <int UNITS>
-__device__ __forceinline__ uint32_t units_total(const uint32_t *tab, int d) {
-    uint32_t run = 0;
-#pragma unroll
-    for (int u = 0; u < UNITS; ++u) run += tab[u * kBuckets + d] >> 16;
-    return run;
-}
+template <int THREADS, int ITEMS, int LANES = rank_lanes<ITEMS>()>
+struct TileRank {
+    static_assert(LANES == 16 || LANES == 32, "half-warp or warp units");
+    static constexpr int kLanes = LANES;
+    static constexpr int kUnits = THREADS / LANES;
+    static constexpr int kShift = LANES == 16 ? 16 : 0;     // where a table word keeps the count
+    static constexpr int kWords = (THREADS / 16) * kBuckets;
+    static constexpr bool kPacked = ITEMS >= 12;
+    static constexpr int kRankRegs = kPacked ? (ITEMS + 1) / 2 : ITEMS;
 
-// replace digit d's unit counts by the units' staging offsets, the first one at the tile start ts
-template <int UNITS>
-__device__ __forceinline__ void units_offsets(uint32_t *tab, int d, uint32_t ts) {
+    __device__ static uint32_t slot0() { return (threadIdx.x / LANES) * LANES * ITEMS + threadIdx.x % LANES; }
+    // the unit's count (later offset) words
+    __device__ static uint32_t *row(uint32_t *tab) { return tab + (threadIdx.x / LANES) * kBuckets; }
+
+    // rank this lane's ITEMS keys within its unit (the unit's masks clear, its counts zero)
+    template <int MODE, typename U>
+    __device__ static void rank(const U (&keys)[ITEMS], uint32_t (&rk)[kRankRegs], uint32_t *tab, uint32_t slot0,
+                                uint32_t tvalid, int pass, uint32_t dmask) {
+        uint32_t *crow = row(tab);
+        const uint32_t bit = 1u << (threadIdx.x % LANES), below = bit - 1u;
 #pragma unroll
-    for (int u = 0; u < UNITS; ++u) {
-        const uint32_t c = tab[u * kBuckets + d] >> 16;
-        tab[u * kBuckets + d] = ts;
-        ts += c;
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t d = slot_digit<MODE>(keys[i], slot0 + uint32_t(LANES) * i, tvalid, pass, dmask);
+            uint32_t r;
+            if constexpr (LANES == 16) {
+                atomicOr(crow + d, bit);
+                __syncwarp();
+                const uint32_t w = crow[d];
+                __syncwarp();
+                const uint32_t peers = w & 0xFFFFu;
+                const uint32_t lower = uint32_t(__popc(peers & below));
+                if (lower == 0) atomicAdd(crow + d, (uint32_t(__popc(peers)) << 16) - peers);
+                __syncwarp();      // the cleared mask is visible to the next item's updates
+                r = (w >> 16) + lower;
+            } else {
+                uint32_t *mrow = tab + (THREADS / 32) * kBuckets + (threadIdx.x / 32) * kBuckets;
+                atomicOr(mrow + d, bit);
+                __syncwarp();
+                const uint32_t peers = mrow[d];
+                __syncwarp();
+                const uint32_t lower = uint32_t(__popc(peers & below));
+                uint32_t before = 0;
+                if (lower == 0) {
+                    before = atomicAdd(crow + d, uint32_t(__popc(peers)));
+                    mrow[d] = 0u;
+                }
+                __syncwarp();
+                r = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1) + lower;
+            }
+            if constexpr (!kPacked) rk[i] = (r << 8) | d;
+            else if (i & 1) rk[i >> 1] |= r << 16;
+            else rk[i >> 1] = r;
+        }
     }
+
+    __device__ static uint32_t rank_of(const uint32_t (&rk)[kRankRegs], int i) {
+        if constexpr (!kPacked) return rk[i] >> 8;
+        else return (rk[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+    }
+
+    // the digit item i was ranked under (slot = its slot in the tile)
+    template <int MODE, typename U>
+    __device__ static uint32_t digit_of_item(const uint32_t (&rk)[kRankRegs], int i, const U &k, uint32_t slot,
+                                             uint32_t tvalid, int pass, uint32_t dmask) {
+        if constexpr (!kPacked) return rk[i] & 0xFFu;
+        else return slot_digit<MODE>(k, slot, tvalid, pass, dmask);
+    }
+
+    // digit d's count in the tile: the sum over the units
+    __device__ static uint32_t total(const uint32_t *tab, int d) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int u = 0; u < kUnits; ++u) run += tab[u * kBuckets + d] >> kShift;
+        return run;
+    }
+
+    // replace digit d's unit counts by the units' staging offsets, the first one at the tile start ts
+    __device__ static void offsets(uint32_t *tab, int d, uint32_t ts) {
+#pragma unroll
+        for (int u = 0; u < kUnits; ++u) {
+            const uint32_t c = tab[u * kBuckets + d] >> kShift;
+            tab[u * kBuckets + d] = ts;
+            ts += c;
+        }
+    }
+
+    // a warp zeroes its units' offset words once its keys are staged, ready for the next tile
+    // (the masks are clear already)
+    __device__ static void clear_own(uint32_t *tab) {
+        uint32_t *rows = tab + (threadIdx.x / 32) * (32 / LANES) * kBuckets;
+        __syncwarp();
+#pragma unroll
+        for (int i = threadIdx.x % 32; i < (32 / LANES) * kBuckets; i += 32) rows[i] = 0u;
+    }
+};
+
+// ---- tile prefetch ---------------------------------------------------------------------------------
+// Ask the L2 for elements [0, count) of p ahead of their loads: one bulk prefetch (the copy engine
+// fetches it while the SM works on the tile before), trimmed inward to 16-byte boundaries so it
+// never touches bytes outside the array.  count * sizeof(T) is one tile: far below 2^32.
+template <typename T>
+__device__ __forceinline__ void prefetch_l2(const T *p, uint64_t count) {
+    uint64_t a = reinterpret_cast<uint64_t>(p), b = a + count * sizeof(T);
+    a = (a + 15u) & ~uint64_t(15);
+    b &= ~uint64_t(15);
+    if (b > a) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(uint32_t(b - a)) : "memory");
 }
 
-// a warp clears the words of its two units once its keys are staged, ready for the next tile
-__device__ __forceinline__ void clear_warp_units(uint32_t *tab) {
-    uint32_t *rows = tab + (threadIdx.x >> 5) * 2u * kBuckets;
-    __syncwarp();
+// the elements of tile `tile` (TILE slots) of an n-element array, read forwards or back to front
+template <int TILE, typename T>
+__device__ __forceinline__ void prefetch_tile(const T *src, uint64_t n, uint32_t tile, bool reverse) {
+    const uint64_t first = uint64_t(tile) * TILE;
+    if (first >= n) return;
+    const uint64_t cnt = (n - first) < uint64_t(TILE) ? (n - first) : uint64_t(TILE);
+    prefetch_l2(reverse ? src + (n - first - cnt) : src + first, cnt);
+}
+
+// ---- decoupled look-back -------------------------------------------------------------------------
+// load the status words of digit d for tiles j, j-1, ..., j-W+1 (none below tile 0)
+template <int W, typename S>
+__device__ __forceinline__ void lookback_load(const S *status, int64_t j, int d, S (&w)[W]) {
 #pragma unroll
-    for (int i = threadIdx.x & 31; i < 2 * kBuckets; i += 32) rows[i] = 0u;
+    for (int q = 0; q < W; ++q) w[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + d) : S(0);
+}
+
+// Walk back from tile `tile` - 1 for digit d, starting from the window `w` already loaded for the
+// tiles tile-1 ... tile-W: add the predecessors' aggregates to `excl` until an inclusive prefix;
+// an unpublished predecessor is re-read (a bounded wait: past spin_limit ns, or once another CTA
+// has aborted, the pass is flagged and the walk gives up).  A window may have been loaded early:
+// a published word only ever changes from aggregate to inclusive, and either adds up to the same
+// prefix.  Returns false if the walk gave up.
+template <int W, typename S>
+__device__ __forceinline__ bool lookback_walk(const S *status, uint32_t tile, int d, S (&w)[W], uint64_t &excl,
+                                              uint32_t *err_word, uint32_t *abort_word, uint64_t spin_limit) {
+    int64_t j = int64_t(tile) - 1;
+    uint32_t spins = 0;
+    uint64_t t0 = 0;
+    while (j >= 0) {
+        int q = 0;
+        for (; q < W && j - q >= 0; ++q) {
+            const uint32_t st = StatusWord<S>::state(w[q]);
+            if (st == kStInvalid) break;
+            excl += StatusWord<S>::value(w[q]);
+            if (st == kStInclusive) return true;
+        }
+        if (q == W) {           // a window of aggregates: keep walking back
+            j -= W;
+        } else {                // wait on the first unpublished predecessor
+            j -= q;
+            if (++spins > 16u) {
+                if (*reinterpret_cast<volatile uint32_t *>(abort_word)) return false;
+                const uint64_t now = globaltimer_ns();
+                if (t0 == 0) t0 = now;
+                else if (now - t0 > spin_limit) {
+                    atomicOr(err_word, kDevTimeout);
+                    atomicExch(abort_word, 1u);
+                    return false;
+                }
+                __nanosleep(32);
+            }
+        }
+        lookback_load(status, j, d, w);
+    }
+    return true;
 }
 
 template <typename U, bool HAS_VAL, int THREADS>
@@ -399,38 +516,38 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
                                            uint32_t stall_tile) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     constexpr int TILE = L::kTile;
-    constexpr int UNITS = THREADS / 16;
+    using R = TileRank<THREADS, ITEMS>;
     U *stage_k = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..17] scan
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t *urow = wofs + (uint32_t(tid) >> 4) * kBuckets;
+    uint32_t *urow = R::row(wofs);
     const uint32_t tile = t.tile;
     const uint64_t n = t.n;
     const uint64_t tbase = uint64_t(tile) * TILE;
     const uint32_t tvalid = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
 
-    // load ITEMS keys per thread: item i of this lane is slot unit_slot0 + 16 i (see rank_unit).
+    // load ITEMS keys per thread: item i of this lane is slot R::slot0() + R::kLanes * i (see TileRank).
     // Slots past the end get digit 255: they rank after every real key of the tile.
     U keys[ITEMS];
     uint64_t vals[HAS_VAL ? ITEMS : 1];
-    uint32_t rk[(ITEMS + 1) / 2];
-    const uint32_t slot0 = unit_slot0<ITEMS>();
+    uint32_t rk[R::kRankRegs];
+    const uint32_t slot0 = R::slot0();
     if (!t.reverse && tvalid == TILE) {
         const U *p = t.src_k + tbase + slot0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
+        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
         if constexpr (HAS_VAL) {
             const uint64_t *q = t.src_v + tbase + slot0;
 #pragma unroll
-            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * 16];
+            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * R::kLanes];
         }
     } else {
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t slot = slot0 + uint32_t(i) * 16u;
+            const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
             const uint64_t gi = tbase + slot;
             const uint64_t si = t.reverse ? (n - 1u - gi) : gi;
             const bool ok = slot < tvalid;
@@ -438,13 +555,13 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
             if constexpr (HAS_VAL) vals[i] = ok ? t.src_v[si] : 0ull;
         }
     }
-    rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalid, pass, dmask);
+    R::template rank<MODE>(keys, rk, wofs, slot0, tvalid, pass, dmask);
     __syncthreads();
 
     // per digit: the tile count; publish the aggregate
     uint32_t count = 0, x = 0, run = 0;
     if (tid < kBuckets) {
-        run = units_total<UNITS>(wofs, tid);
+        run = R::total(wofs, tid);
         count = run;
         if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalid;   // the padding slots
         if (tile != stall_tile)
@@ -463,50 +580,15 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
         uint32_t before = 0;
         for (int i = 0; i < warp; ++i) before += misc[2 + i];
         const uint32_t ts = before + x - run;          // tile start of digit tid
-        units_offsets<UNITS>(wofs, tid, ts);
-    // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
+        R::offsets(wofs, tid, ts);
+        // decoupled look-back for digit tid: read predecessors kWin at a time (bounded wait)
         uint64_t excl = 0;
         bool bad = false;
         if (tile > 0) {
-            int64_t j = int64_t(tile) - 1;
-            uint32_t spins = 0;
-            uint64_t t0 = 0;
-            bool done = false;
-            while (!done && j >= 0) {
-                constexpr int kWin = sizeof(U) <= 4 ? 4 : 8;   // measured best per key size
-                S w4[kWin];
-#pragma unroll
-                for (int q = 0; q < kWin; ++q)
-                    w4[q] = (j - q >= 0) ? ld_relaxed(t.status + size_t(j - q) * kBuckets + tid) : S(0);
-                int q = 0;
-                for (; q < kWin && j - q >= 0; ++q) {
-                    const uint32_t st = StatusWord<S>::state(w4[q]);
-                    if (st == kStInvalid) break;
-                    excl += StatusWord<S>::value(w4[q]);
-                    if (st == kStInclusive) {
-                        done = true;
-                        break;
-                    }
-                }
-                if (done) break;
-                if (q == kWin) {       // a window of aggregates: keep walking back
-                    j -= kWin;
-                    continue;
-                }
-                j -= q;                // wait on the first unpublished predecessor
-                if (++spins > 16u) {
-                    if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
-                    const uint64_t now = globaltimer_ns();
-                    if (t0 == 0) t0 = now;
-                    else if (now - t0 > spin_limit) {
-                        atomicOr(err_word, kDevTimeout);
-                        atomicExch(abort_word, 1u);
-                        bad = true;
-                        break;
-                    }
-                    __nanosleep(32);
-                }
-            }
+            constexpr int kWin = sizeof(U) <= 4 ? 4 : 8;   // measured best per key size
+            S w[kWin];
+            lookback_load(t.status, int64_t(tile) - 1, tid, w);
+            bad = !lookback_walk(t.status, tile, tid, w, excl, err_word, abort_word, spin_limit);
             if (tile != stall_tile)
                 st_relaxed(t.status + size_t(tile) * kBuckets + tid,
                            StatusWord<S>::make(kStInclusive, excl + count));
@@ -520,12 +602,12 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     // stage the tile in shared memory, sorted by digit (padding slots land past tvalid)
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalid, pass, dmask);
-        const uint32_t pos = urow[d] + unit_rank<ITEMS>(rk, i);
+        const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalid, pass, dmask);
+        const uint32_t pos = urow[d] + R::rank_of(rk, i);
         stage_k[pos] = keys[i];
         if constexpr (HAS_VAL) stage_v[pos] = vals[i];
     }
-    clear_warp_units(wofs);
+    R::clear_own(wofs);
     __syncthreads();
     // write out: consecutive threads take consecutive slots of a bucket run
     if (!tile_bad) {
@@ -588,8 +670,16 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
     sweep_init_smem<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem);
     for (;;) {
         if (threadIdx.x == 0) {
-            misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
+            const uint32_t tile = atomicAdd(&ctrl->tile_counter[pass], 1u);
+            misc[0] = tile;
             misc[1] = 0;
+            // the tile one grid stride on is about the next one any CTA claims: its data go to L2 now
+            const uint32_t ahead = tile + gridDim.x;
+            if (ahead < num_tiles) {
+                constexpr int TILE = L::kTile;
+                prefetch_tile<TILE>(t.src_k, n, ahead, t.reverse);
+                if constexpr (HAS_VAL) prefetch_tile<TILE>(t.src_v, n, ahead, t.reverse);
+            }
         }
         __syncthreads();
         const uint32_t tile = misc[0];
@@ -614,15 +704,15 @@ template <typename U, int THREADS, int ITEMS>
 struct PipeSmem {
     static constexpr int kTile = THREADS * ITEMS;
     static constexpr int kWarps = THREADS / 32;
-    static constexpr int kUnits = THREADS / 16;
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
-    static constexpr size_t kOffUnits = (kStageK + 15) & ~size_t(15);  // u32 [UNITS][256]
-    static constexpr size_t kOffGofs = kOffUnits + size_t(kUnits) * kBuckets * 4;   // i64 [256] of tile A
+    static constexpr size_t kOffUnits = (kStageK + 15) & ~size_t(15);  // u32: the TileRank table
+    static constexpr size_t kOffGofs = kOffUnits + size_t(THREADS / 16) * kBuckets * 4;   // i64 [256] of tile A
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;     // u64 [256]
     static constexpr size_t kOffTs = kOffBstart + kBuckets * 8;       // u32 [2][256] tile starts
     static constexpr size_t kOffCnt = kOffTs + 2 * kBuckets * 4;      // u32 [2][256] tile counts
     static constexpr size_t kOffMisc = kOffCnt + 2 * kBuckets * 4;    // u32 [32]
-    static constexpr size_t kBytes = kOffMisc + 128;
+    static constexpr size_t kOffAux = kOffMisc + 128;                 // 128 B for the kernel's own use
+    static constexpr size_t kBytes = kOffAux + 128;
 };
 
 template <typename U, int MODE, int THREADS, int ITEMS, typename S>
@@ -633,7 +723,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     using L = PipeSmem<U, THREADS, ITEMS>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
-    constexpr int UNITS = L::kUnits;
+    using R = TileRank<THREADS, ITEMS>;
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
@@ -653,11 +743,11 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t *err_word = &ctrl->error;
     uint32_t *abort_word = &ctrl->abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t *urow = utab + (uint32_t(tid) >> 4) * kBuckets;
-    const uint32_t slot0 = unit_slot0<ITEMS>();
+    uint32_t *urow = R::row(utab);
+    const uint32_t slot0 = R::slot0();
 
     for (int i = tid; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
-    for (int i = tid; i < UNITS * kBuckets; i += THREADS) utab[i] = 0u;
+    for (int i = tid; i < R::kWords; i += THREADS) utab[i] = 0u;
     if (tid == 0) {
         misc[0] = atomicAdd(&ctrl->tile_counter[pass], 1u);
         misc[1] = 0u;
@@ -673,11 +763,18 @@ __global__ void __launch_bounds__(THREADS, 2)
         uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
         uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
         uint32_t next = 0xFFFFFFFFu;
-        if (hasB && tid == 0) next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B
+        if (hasB && tid == 0) {
+            next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B: its keys go to L2 now
+            if (next < num_tiles) prefetch_tile<TILE>(src, n, next, reverse);
+        }
+        // the look-back threads load A's first window now: the loads complete while B is ranked
+        constexpr int kWin = sizeof(U) <= 8 ? 4 : 8;   // measured best per key size
+        S lbw[kWin];
+        if (hasA && tid >= kBuckets && tileA > 0) lookback_load(status, int64_t(tileA) - 1, tid - kBuckets, lbw);
 
         // ---- (1) load and rank tile B (half-warp units, as in sweep_tile)
         U keys[ITEMS];
-        uint32_t rk[(ITEMS + 1) / 2];
+        uint32_t rk[R::kRankRegs];
         uint32_t tvalidB = 0;
         if (hasB) {
             const uint64_t tbase = uint64_t(tileB) * TILE;
@@ -685,16 +782,16 @@ __global__ void __launch_bounds__(THREADS, 2)
             if (!reverse && tvalidB == TILE) {
                 const U *p = src + tbase + slot0;
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
             } else {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * 16u;
+                    const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
                     const uint64_t gi = tbase + slot;
                     keys[i] = slot < tvalidB ? src[reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
                 }
             }
-            rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalidB, pass, dmask);
+            R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, dmask);
         }
         __syncthreads();                                                        // barrier 1
 
@@ -703,7 +800,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         uint32_t x = 0, run = 0;
         if (tid < kBuckets) {
             if (hasB) {
-                run = units_total<UNITS>(utab, tid);
+                run = R::total(utab, tid);
                 uint32_t count = run;
                 if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
                 cntB[tid] = count;
@@ -724,45 +821,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             uint64_t excl = 0;
             bool bad = false;
             if (tileA > 0) {
-                int64_t j = int64_t(tileA) - 1;
-                uint32_t spins = 0;
-                uint64_t t0 = 0;
-                bool done = false;
-                while (!done && j >= 0) {
-                    constexpr int kWin = sizeof(U) <= 4 ? 4 : (sizeof(U) == 8 ? 2 : 8);   // measured best per key size
-                    S w4[kWin];
-#pragma unroll
-                    for (int q = 0; q < kWin; ++q)
-                        w4[q] = (j - q >= 0) ? ld_relaxed(status + size_t(j - q) * kBuckets + d) : S(0);
-                    int q = 0;
-                    for (; q < kWin && j - q >= 0; ++q) {
-                        const uint32_t st = StatusWord<S>::state(w4[q]);
-                        if (st == kStInvalid) break;
-                        excl += StatusWord<S>::value(w4[q]);
-                        if (st == kStInclusive) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (done) break;
-                    if (q == kWin) {
-                        j -= kWin;
-                        continue;
-                    }
-                    j -= q;
-                    if (++spins > 16u) {
-                        if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
-                        const uint64_t now = globaltimer_ns();
-                        if (t0 == 0) t0 = now;
-                        else if (now - t0 > spin_limit) {
-                            atomicOr(err_word, kDevTimeout);
-                            atomicExch(abort_word, 1u);
-                            bad = true;
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
+                bad = !lookback_walk(status, tileA, d, lbw, excl, err_word, abort_word, spin_limit);
                 if (tileA != stall_tile)
                     st_relaxed(status + size_t(tileA) * kBuckets + d, StatusWord<S>::make(kStInclusive, excl + count));
             }
@@ -776,7 +835,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
             const uint32_t ts = before + x - run;
-            units_offsets<UNITS>(utab, tid, ts);
+            R::offsets(utab, tid, ts);
             tsB[tid] = ts;
         }
         if (hasA && misc[1] == 0u && tileA != stall_tile) {
@@ -802,10 +861,10 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (hasB) {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalidB, pass, dmask);
-                stage[urow[d] + unit_rank<ITEMS>(rk, i)] = keys[i];
+                const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalidB, pass, dmask);
+                stage[urow[d] + R::rank_of(rk, i)] = keys[i];
             }
-            clear_warp_units(utab);
+            R::clear_own(utab);
         }
         if (tid == 0) {
             misc[0] = next;

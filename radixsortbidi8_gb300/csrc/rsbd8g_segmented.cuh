@@ -44,6 +44,7 @@ struct SegArgs {
     uint32_t *small_seg;      // [nsegs]
     uint32_t *seg_hist;       // [nlarge_max][P][256]: counts, then bucket starts
     uint32_t *seg_mask;       // [nlarge_max]: surviving digits
+    uint32_t *tile_seg;       // [tiles_max]: the large segment (list index) of each tile, by k_seg_hist
     // pointer-table form: segment s lives at ptr_in[s] / ptr_out[s] / ptr_buf[s] (separate arrays;
     // offsets then only give the lengths); null: segment s is at offsets[s] of in / out / buf
     const uint64_t *ptr_in;
@@ -144,6 +145,7 @@ __device__ __forceinline__ uint32_t seg_of_tile(const uint32_t *tbase, uint32_t 
 }
 
 // all digit histograms of every large segment; CTA c reads a contiguous run of tiles in order
+// (and records the segment of each of those tiles for the scatter passes)
 template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__restrict__ in) {
     constexpr int P = int(sizeof(U));
@@ -166,6 +168,7 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         const uint64_t len = seg_len(a.offsets, seg);
         const U *src = seg_ptr(a, a.ptr_in, in, seg);
         const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
+        for (uint32_t x = gt + threadIdx.x; x < tend; x += THREADS) a.tile_seg[x] = idx;
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
         const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
         constexpr int UNR = 8;                           // loads in flight per thread
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);
     SegControl *c = a.ctrl;
     if (c->abort) return;
-    const uint32_t T = c->ntiles, nl = c->nlarge;
+    const uint32_t T = c->ntiles;
     const uint64_t spin_limit = a.spin_limit_ns;
     sweep_init_smem<U, MODE, false, THREADS, ITEMS, uint32_t>(smem);
     for (;;) {
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
         __syncthreads();
         const uint32_t gt = misc[0];
         if (gt >= T) break;
-        const uint32_t idx = seg_of_tile(a.large_tbase, nl, gt);
+        const uint32_t idx = a.tile_seg[gt];
         const uint32_t mask = a.seg_mask[idx];
         if (!((mask >> pass) & 1u)) {        // this digit is skipped for the segment
             __syncthreads();
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
 // destination, length, look-back words and bucket starts; a tile whose segment skips this digit is
 // passed over.
 struct SegPipeTile {
-    const void *src;
+    const void *src;            // null: the tile's segment skips this digit (the tile is passed over)
     void *dst;
     const uint32_t *bs;        // bucket starts of this pass for the segment (global)
     uint32_t *status;          // look-back words of the segment's tile 0
@@ -303,9 +306,10 @@ struct SegPipeTile {
 
 template <typename U>
 __device__ __forceinline__ bool seg_pipe_tile(const SegArgs &a, int pass, int passes, const U *in, U *out, U *buf,
-                                              uint32_t *status, uint32_t gt, uint32_t nl, SegPipeTile &t) {
-    const uint32_t idx = seg_of_tile(a.large_tbase, nl, gt);
+                                              uint32_t *status, uint32_t gt, SegPipeTile &t) {
+    const uint32_t idx = a.tile_seg[gt];
     const uint32_t mask = a.seg_mask[idx];
+    t.src = nullptr;
     if (!((mask >> pass) & 1u)) return false;          // this digit is skipped for the segment
     const uint32_t seg = a.large_seg[idx];
     const int k = __popc(mask), i = __popc(mask & ((1u << pass) - 1u)) + 1;
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     using L = PipeSmem<U, THREADS, ITEMS>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
-    constexpr int UNITS = L::kUnits;
+    using R = TileRank<THREADS, ITEMS>;
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
@@ -339,18 +343,24 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] next tile [1] bad [2..9] scan
     SegControl *c = a.ctrl;
     if (c->abort) return;
-    const uint32_t T = c->ntiles, nl = c->nlarge;
+    // the descriptors of the claimed tiles, two slots used in turn: thread 0 looks a tile up once
+    // when it claims it and the CTA reads the descriptor from here one iteration later
+    static_assert(2 * sizeof(SegPipeTile) <= 128, "descriptor slots fit the auxiliary area");
+    SegPipeTile *slots = reinterpret_cast<SegPipeTile *>(smem + L::kOffAux);
+    const uint32_t T = c->ntiles;
     const uint64_t spin_limit = a.spin_limit_ns;
     uint32_t *err_word = &c->error;
     uint32_t *abort_word = &c->abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t *urow = utab + (uint32_t(tid) >> 4) * kBuckets;
-    const uint32_t slot0 = unit_slot0<ITEMS>();
+    uint32_t *urow = R::row(utab);
+    const uint32_t slot0 = R::slot0();
 
-    for (int i = tid; i < UNITS * kBuckets; i += THREADS) utab[i] = 0u;
+    for (int i = tid; i < R::kWords; i += THREADS) utab[i] = 0u;
     if (tid == 0) {
-        misc[0] = atomicAdd(&c->tile_counter[pass], 1u);
+        const uint32_t g = atomicAdd(&c->tile_counter[pass], 1u);
+        misc[0] = g;
         misc[1] = 0u;
+        if (g < T) seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, g, slots[0]);
     }
     __syncthreads();
     uint32_t gtB = misc[0];
@@ -358,17 +368,27 @@ __global__ void __launch_bounds__(THREADS, 2)
     SegPipeTile A{}, B{};
     uint32_t tvalidA = 0;
     int par = 0;
-    for (;;) {
+    for (uint32_t it = 0;; ++it) {
         const bool claimed = gtB < T;
         if (!hasA && !claimed) break;
-        const bool hasB = claimed && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, gtB, nl, B);
+        if (claimed) B = slots[it & 1u];
+        const bool hasB = claimed && B.src != nullptr;
         uint32_t *tsB = tsall + par * kBuckets, *tsA = tsall + (par ^ 1) * kBuckets;
         uint32_t *cntB = cntall + par * kBuckets, *cntA = cntall + (par ^ 1) * kBuckets;
         uint32_t next = 0xFFFFFFFFu;
-        if (claimed && tid == 0) next = atomicAdd(&c->tile_counter[pass], 1u);
+        if (claimed && tid == 0) {
+            next = atomicAdd(&c->tile_counter[pass], 1u);   // the tile after B: its keys go to L2 now
+            SegPipeTile &N = slots[(it & 1u) ^ 1u];
+            if (next < T && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, next, N))
+                prefetch_tile<TILE>(static_cast<const U *>(N.src), N.n, N.tile, N.reverse != 0);
+        }
+        // the look-back threads load A's first window now: the loads complete while B is ranked
+        constexpr int kWin = 4;
+        uint32_t lbw[kWin];
+        if (hasA && tid >= kBuckets && A.tile > 0) lookback_load(A.status, int64_t(A.tile) - 1, tid - kBuckets, lbw);
 
         U keys[ITEMS];
-        uint32_t rk[(ITEMS + 1) / 2];
+        uint32_t rk[R::kRankRegs];
         uint32_t tvalidB = 0;
         if (hasB) {
             const U *src = static_cast<const U *>(B.src);
@@ -378,23 +398,23 @@ __global__ void __launch_bounds__(THREADS, 2)
             if (!B.reverse && tvalidB == TILE) {
                 const U *p = src + tbase + slot0;
 #pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * 16];
+                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
             } else {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * 16u;
+                    const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
                     const uint64_t gi = tbase + slot;
                     keys[i] = slot < tvalidB ? src[B.reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
                 }
             }
-            rank_unit<MODE, ITEMS>(keys, rk, urow, slot0, tvalidB, pass, a.dmask);
+            R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, a.dmask);
         }
         __syncthreads();                                                        // barrier 1
 
         uint32_t x = 0, run = 0;
         if (tid < kBuckets) {
             if (hasB) {
-                run = units_total<UNITS>(utab, tid);
+                run = R::total(utab, tid);
                 uint32_t count = run;
                 if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
                 cntB[tid] = count;
@@ -415,45 +435,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             uint64_t excl = 0;
             bool bad = false;
             if (A.tile > 0) {
-                int64_t j = int64_t(A.tile) - 1;
-                uint32_t spins = 0;
-                uint64_t t0 = 0;
-                bool done = false;
-                while (!done && j >= 0) {
-                    constexpr int kWin = sizeof(U) <= 4 ? 4 : 2;
-                    uint32_t w4[kWin];
-#pragma unroll
-                    for (int q = 0; q < kWin; ++q)
-                        w4[q] = (j - q >= 0) ? ld_relaxed(A.status + size_t(j - q) * kBuckets + d) : 0u;
-                    int q = 0;
-                    for (; q < kWin && j - q >= 0; ++q) {
-                        const uint32_t st = StatusWord<uint32_t>::state(w4[q]);
-                        if (st == kStInvalid) break;
-                        excl += StatusWord<uint32_t>::value(w4[q]);
-                        if (st == kStInclusive) {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (done) break;
-                    if (q == kWin) {
-                        j -= kWin;
-                        continue;
-                    }
-                    j -= q;
-                    if (++spins > 16u) {
-                        if (*reinterpret_cast<volatile uint32_t *>(abort_word)) { bad = true; break; }
-                        const uint64_t now = globaltimer_ns();
-                        if (t0 == 0) t0 = now;
-                        else if (now - t0 > spin_limit) {
-                            atomicOr(err_word, kDevTimeout);
-                            atomicExch(abort_word, 1u);
-                            bad = true;
-                            break;
-                        }
-                        __nanosleep(32);
-                    }
-                }
+                bad = !lookback_walk(A.status, A.tile, d, lbw, excl, err_word, abort_word, spin_limit);
                 if (A.tile != stall_tile)
                     st_relaxed(A.status + size_t(A.tile) * kBuckets + d,
                                StatusWord<uint32_t>::make(kStInclusive, excl + count));
@@ -467,7 +449,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
             const uint32_t ts = before + x - run;
-            units_offsets<UNITS>(utab, tid, ts);
+            R::offsets(utab, tid, ts);
             tsB[tid] = ts;
         }
         if (hasA && misc[1] == 0u && A.tile != stall_tile) {
@@ -484,10 +466,10 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (hasB) {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t d = slot_digit<MODE>(keys[i], slot0 + 16u * i, tvalidB, pass, a.dmask);
-                stage[urow[d] + unit_rank<ITEMS>(rk, i)] = keys[i];
+                const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalidB, pass, a.dmask);
+                stage[urow[d] + R::rank_of(rk, i)] = keys[i];
             }
-            clear_warp_units(utab);
+            R::clear_own(utab);
         }
         if (tid == 0) {
             misc[0] = next;

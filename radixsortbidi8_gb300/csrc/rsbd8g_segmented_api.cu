@@ -37,7 +37,8 @@ rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, cons
     L->large_tbase = L->large_seg + up(L->nlarge_max * 4);
     L->small_seg = L->large_tbase + up((L->nlarge_max + 1) * 4);
     L->seg_mask = L->small_seg + up(nsegs * 4);
-    L->status = L->seg_mask + up(L->nlarge_max * 4);
+    L->tile_seg = L->seg_mask + up(L->nlarge_max * 4);
+    L->status = L->tile_seg + up(L->tiles_max * 4);
     L->status_bytes = up(L->tiles_max * kBuckets * 4);
     L->total = L->status + L->status_bytes;
     return RSBD8G_OK;
@@ -105,6 +106,7 @@ static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, siz
     a.small_seg = reinterpret_cast<uint32_t *>(sc + L.small_seg);
     a.seg_hist = reinterpret_cast<uint32_t *>(sc + L.seg_hist);
     a.seg_mask = reinterpret_cast<uint32_t *>(sc + L.seg_mask);
+    a.tile_seg = reinterpret_cast<uint32_t *>(sc + L.tile_seg);
     a.ptr_in = in_ptrs;
     a.ptr_out = out_ptrs;
     a.ptr_buf = buf_ptrs;
