@@ -91,6 +91,13 @@ enum {
 /* diagnostics only: the allocating forms act as if their device allocation failed (the one
  * failure the reference reports, as a false return): RSBD8G_ERR_NO_MEMORY, arrays untouched */
 #define RSBD8G_FLAG_DIAG_NOMEM 2u
+/* the caller states that every array of the call -- in the pointer-table segmented form also every
+ * array the tables point to -- is device memory (cudaMalloc, a CUDA memory pool).  The scatter
+ * passes then prefetch each tile into L2 with a bulk copy before loading it.  The plain forms and
+ * the contiguous segmented form find this out themselves (cudaPointerGetAttributes); the
+ * pointer-table form prefetches only with this flag.  Managed and host memory are read with plain
+ * loads alone. */
+#define RSBD8G_FLAG_DEVICE_ARRAYS 4u
 
 typedef struct rsbd8g_desc {
     uint32_t key_bytes;     /* 1, 2, 4, 8 or 16 (16: not in the segmented and serving entry points) */
@@ -98,7 +105,7 @@ typedef struct rsbd8g_desc {
     uint32_t mode;          /* rsbd8::sortingmode value */
     uint32_t direction;     /* rsbd8::sortingdirection value */
     uint32_t indirection;   /* RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2 */
-    uint32_t flags;         /* 0, or RSBD8G_FLAG_* diagnostics */
+    uint32_t flags;         /* 0, or RSBD8G_FLAG_* */
     int64_t offset1;        /* RSBD8G_MEMBER*: byte offset of the key (or second pointer) in each object */
     int64_t offset2;        /* RSBD8G_MEMBER2: byte offset of the key behind the second pointer */
 } rsbd8g_desc;

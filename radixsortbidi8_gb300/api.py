@@ -36,6 +36,7 @@ WIDE_KEY_KINDS = {"u128": KIND_UNSIGNED, "i128": KIND_SIGNED, "f128": KIND_FLOAT
 DIRECT, MEMBER, MEMBER2 = 0, 1, 2
 FLAG_DIAG_STALL = 1
 FLAG_DIAG_NOMEM = 2
+FLAG_DEVICE_ARRAYS = 4        # every array is device memory (include/rsbd8g.h)
 
 STATUS = {0: "ok", 1: "bad argument", 2: "device allocation failed", 3: "CUDA runtime error",
           4: "device-side wait timed out", 5: "device-side fault flag", 6: "count too large",

@@ -162,6 +162,7 @@ rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
     r->off1 = d->offset1;
     r->off2 = d->offset2;
     r->flags = d->flags;
+    r->prefetch = 0;
     r->keys = nullptr;
     return RSBD8G_OK;
 }
@@ -187,8 +188,24 @@ Layout layout_for(const Resolved &r, uint64_t n) {
     return L;
 }
 
-rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
+bool device_memory(const void *p) {
+    if (!p) return true;                  // an absent array takes no part
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();         // not a pointer CUDA accepts: reset the (non-sticky) error
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice;
+}
+
+rsbd8g_status enqueue_sort(const Resolved &rin, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
                            void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
+    // the scatter passes prefetch tiles into L2 with bulk copies only from device memory
+    // (cudaMalloc, memory pools); managed and host memory is read with plain loads alone
+    Resolved r = rin;
+    r.prefetch = (r.flags & RSBD8G_FLAG_DEVICE_ARRAYS) ||
+                 (device_memory(in) && device_memory(out) && device_memory(buf) &&
+                  (!r.indirect || device_memory(scratch)));
     if (n > kMaxCount) return RSBD8G_ERR_TOO_LARGE;
     const Layout L = layout_for(r, n);
     if (!scratch || scratch_bytes < L.total) return RSBD8G_ERR_BAD_ARG;

@@ -57,7 +57,7 @@ struct Control {
     void *copy_dst;
     uint64_t copy_elem_bytes;
     uint32_t stall_tile;   // diagnostics: this tile never publishes (0xFFFFFFFF = off)
-    uint32_t pad;
+    uint32_t prefetch;     // 1: every array is device memory, so tiles may be prefetched into L2
     uint64_t spin_limit_ns;
     PassPlan plan[kMaxPasses];
 };

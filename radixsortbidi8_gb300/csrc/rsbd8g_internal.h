@@ -20,6 +20,7 @@ struct Resolved {
     uint32_t elem_bytes;  // bytes per array element (key bytes, or 8 for object pointers)
     uint32_t indirect;    // RSBD8G_DIRECT / RSBD8G_MEMBER / RSBD8G_MEMBER2
     uint32_t flags;
+    uint32_t prefetch;    // every array of the call is device memory (tiles may be prefetched into L2)
     int64_t off1, off2;
     const void *keys;     // RSBD8G_KEYED: the caller's key array
 };
@@ -109,6 +110,8 @@ RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k4)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k8)
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
+// p is device memory (cudaMalloc, a memory pool, a __device__ array); null counts as such
+bool device_memory(const void *p);
 Layout layout_for(const Resolved &r, uint64_t n);
 rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
                            void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);

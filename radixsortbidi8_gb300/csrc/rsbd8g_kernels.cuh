@@ -187,6 +187,7 @@ struct PlanArgs {
     uint32_t indirect;
     uint32_t stall_tile;
     uint32_t passes;       // digits of the key
+    uint32_t prefetch;     // every array is device memory (Control::prefetch)
 };
 
 // one CTA of 256 threads
@@ -219,6 +220,7 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
     ctrl->active_passes = uint32_t(k);
     ctrl->spin_limit_ns = a.spin_limit_ns;
     ctrl->stall_tile = a.stall_tile;
+    ctrl->prefetch = a.prefetch;
     ctrl->copy_mode = kCopyNone;
     ctrl->copy_elem_bytes = a.elem_bytes;
     const void *cur = a.in;               // where the data (values for indirection) is
@@ -666,6 +668,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
     t.reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
+    const bool prefetch = ctrl->prefetch != 0;
     for (int i = threadIdx.x; i < kBuckets; i += THREADS) bstart[i] = bstart_all[pass * kBuckets + i];
     sweep_init_smem<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem);
     for (;;) {
@@ -675,7 +678,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
             misc[1] = 0;
             // the tile one grid stride on is about the next one any CTA claims: its data go to L2 now
             const uint32_t ahead = tile + gridDim.x;
-            if (ahead < num_tiles) {
+            if (prefetch && ahead < num_tiles) {
                 constexpr int TILE = L::kTile;
                 prefetch_tile<TILE>(t.src_k, n, ahead, t.reverse);
                 if constexpr (HAS_VAL) prefetch_tile<TILE>(t.src_v, n, ahead, t.reverse);
@@ -740,6 +743,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     const bool reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
+    const bool prefetch = ctrl->prefetch != 0;
     uint32_t *err_word = &ctrl->error;
     uint32_t *abort_word = &ctrl->abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -765,7 +769,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         uint32_t next = 0xFFFFFFFFu;
         if (hasB && tid == 0) {
             next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B: its keys go to L2 now
-            if (next < num_tiles) prefetch_tile<TILE>(src, n, next, reverse);
+            if (prefetch && next < num_tiles) prefetch_tile<TILE>(src, n, next, reverse);
         }
         // the look-back threads load A's first window now: the loads complete while B is ranked
         constexpr int kWin = sizeof(U) <= 8 ? 4 : 8;   // measured best per key size

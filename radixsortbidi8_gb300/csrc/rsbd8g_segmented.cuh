@@ -51,6 +51,7 @@ struct SegArgs {
     const uint64_t *ptr_out;
     const uint64_t *ptr_buf;
     uint64_t spin_limit_ns;   // bound of every look-back wait
+    uint32_t prefetch;        // every array is device memory: tiles may be prefetched into L2
 };
 
 __device__ __forceinline__ uint64_t seg_len(const uint64_t *off, uint32_t s) { return off[s + 1] - off[s]; }
@@ -379,7 +380,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (claimed && tid == 0) {
             next = atomicAdd(&c->tile_counter[pass], 1u);   // the tile after B: its keys go to L2 now
             SegPipeTile &N = slots[(it & 1u) ^ 1u];
-            if (next < T && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, next, N))
+            if (next < T && seg_pipe_tile<U>(a, pass, passes, in, out, buf, status, next, N) && a.prefetch)
                 prefetch_tile<TILE>(static_cast<const U *>(N.src), N.n, N.tile, N.reverse != 0);
         }
         // the look-back threads load A's first window now: the loads complete while B is ranked

@@ -111,6 +111,10 @@ static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, siz
     a.ptr_out = out_ptrs;
     a.ptr_buf = buf_ptrs;
     a.spin_limit_ns = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 200000000ull : 1000000000ull;
+    // tiles are prefetched into L2 only from device memory: the contiguous form checks its three
+    // arrays, the pointer-table form relies on the caller's RSBD8G_FLAG_DEVICE_ARRAYS
+    a.prefetch = (r.flags & RSBD8G_FLAG_DEVICE_ARRAYS) ||
+                 (!in_ptrs && device_memory(input) && device_memory(output) && device_memory(buffer));
     switch (r.key_bytes) {
         case 1: e = launch_segmented_k1(r, a, L, sc, input, output, buffer, s); break;
         case 2: e = launch_segmented_k2(r, a, L, sc, input, output, buffer, s); break;

@@ -24,6 +24,10 @@
 
 #include "rsbd8g.h"
 
+namespace rsbd8g {
+bool device_memory(const void *p);   // rsbd8g_api.cu
+}
+
 namespace {
 
 constexpr size_t kAlignArena = 256;
@@ -90,6 +94,7 @@ struct Request {
     size_t buf_off = 0, buf_bytes = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
     int state = 0;   // 0 pending, 1 running, 2 done
+    bool device = false;   // input and output are device memory
     rsbd8g_status status = RSBD8G_OK;
 };
 
@@ -284,9 +289,14 @@ struct Server {
     // issue a formed batch on its stream (`mu` NOT held: CUDA calls only)
     void issue(Batch *b) {
         const size_t n = b->reqs.size();
-        const rsbd8g_desc key = b->reqs.front()->desc;
+        rsbd8g_desc key = b->reqs.front()->desc;
         uint64_t *ho = b->host_tables, *hi = ho + (n + 1), *hout = hi + n, *hbuf = hout + n;
         ho[0] = 0;
+        // the buffers are in the arena (device memory): the batch may prefetch tiles into L2 when
+        // every request's arrays are device memory too
+        bool device = true;
+        for (size_t i = 0; i < n; ++i) device = device && b->reqs[i]->device;
+        if (device) key.flags |= RSBD8G_FLAG_DEVICE_ARRAYS;
         for (size_t i = 0; i < n; ++i) {
             ho[i + 1] = ho[i] + b->reqs[i]->count;
             hi[i] = reinterpret_cast<uint64_t>(b->reqs[i]->in);
@@ -405,6 +415,7 @@ RSBD8G_API rsbd8g_status rsbd8g_server_submit(rsbd8g_server *h, const rsbd8g_des
     r->count = count;
     r->in = input;
     r->out = output;
+    r->device = rsbd8g::device_memory(input) && rsbd8g::device_memory(output);
     r->t_submit = now_s();
     {
         std::lock_guard<std::mutex> g(s.mu);
