@@ -693,7 +693,7 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
     }
 }
 
-// ---- the pipelined scatter pass (direct keys) -------------------------------------------------
+// ---- the pipelined scatter pass -----------------------------------------------------------------
 // Tile B is loaded and ranked while tile A, ranked one iteration earlier and staged in shared
 // memory, waits for its look-back; A's look-back then runs in threads 256..511 while threads 0..255
 // scan B's counts, and A is written out while B's offsets are finished.  The look-back wait of one
@@ -703,12 +703,13 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
 // nothing, so the lowest unresolved tile always resolves.  Tile B's unit words are scanned into
 // offsets in (3a) and cleared by each warp once B is staged in (4), so one table serves every tile.
 
-template <typename U, int THREADS, int ITEMS>
+template <typename U, int THREADS, int ITEMS, bool HAS_VAL = false>
 struct PipeSmem {
     static constexpr int kTile = THREADS * ITEMS;
     static constexpr int kWarps = THREADS / 32;
     static constexpr size_t kStageK = size_t(kTile) * sizeof(U);
-    static constexpr size_t kOffUnits = (kStageK + 15) & ~size_t(15);  // u32: the TileRank table
+    static constexpr size_t kOffV = (kStageK + 15) & ~size_t(15);     // u64 [TILE]: the staged pointers
+    static constexpr size_t kOffUnits = kOffV + (HAS_VAL ? size_t(kTile) * 8 : 0);  // u32: the TileRank table
     static constexpr size_t kOffGofs = kOffUnits + size_t(THREADS / 16) * kBuckets * 4;   // i64 [256] of tile A
     static constexpr size_t kOffBstart = kOffGofs + kBuckets * 8;     // u64 [256]
     static constexpr size_t kOffTs = kOffBstart + kBuckets * 8;       // u32 [2][256] tile starts
@@ -718,17 +719,18 @@ struct PipeSmem {
     static constexpr size_t kBytes = kOffAux + 128;
 };
 
-template <typename U, int MODE, int THREADS, int ITEMS, typename S>
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, 2)
     k_onesweep_pipe(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
                     S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
-    using L = PipeSmem<U, THREADS, ITEMS>;
+    using L = PipeSmem<U, THREADS, ITEMS, HAS_VAL>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
     using R = TileRank<THREADS, ITEMS>;
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
+    uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
@@ -739,7 +741,9 @@ __global__ void __launch_bounds__(THREADS, 2)
     const PassPlan plan = ctrl->plan[pass];
     if (!plan.active) return;
     const U *src = static_cast<const U *>(plan.src_keys);
-    U *dst = static_cast<U *>(plan.dst_keys);
+    U *dst = static_cast<U *>(plan.dst_keys);       // null: keys are dropped (last pass of an indirect sort)
+    const uint64_t *src_v = static_cast<const uint64_t *>(plan.src_vals);
+    uint64_t *dst_v = static_cast<uint64_t *>(plan.dst_vals);
     const bool reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
@@ -769,15 +773,19 @@ __global__ void __launch_bounds__(THREADS, 2)
         uint32_t next = 0xFFFFFFFFu;
         if (hasB && tid == 0) {
             next = atomicAdd(&ctrl->tile_counter[pass], 1u);   // the tile after B: its keys go to L2 now
-            if (prefetch && next < num_tiles) prefetch_tile<TILE>(src, n, next, reverse);
+            if (prefetch && next < num_tiles) {
+                prefetch_tile<TILE>(src, n, next, reverse);
+                if constexpr (HAS_VAL) prefetch_tile<TILE>(src_v, n, next, reverse);
+            }
         }
         // the look-back threads load A's first window now: the loads complete while B is ranked
         constexpr int kWin = sizeof(U) <= 8 ? 4 : 8;   // measured best per key size
         S lbw[kWin];
         if (hasA && tid >= kBuckets && tileA > 0) lookback_load(status, int64_t(tileA) - 1, tid - kBuckets, lbw);
 
-        // ---- (1) load and rank tile B (half-warp units, as in sweep_tile)
+        // ---- (1) load and rank tile B (the units of sweep_tile)
         U keys[ITEMS];
+        uint64_t vals[HAS_VAL ? ITEMS : 1];
         uint32_t rk[R::kRankRegs];
         uint32_t tvalidB = 0;
         if (hasB) {
@@ -787,12 +795,19 @@ __global__ void __launch_bounds__(THREADS, 2)
                 const U *p = src + tbase + slot0;
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
+                if constexpr (HAS_VAL) {
+                    const uint64_t *q = src_v + tbase + slot0;
+#pragma unroll
+                    for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * R::kLanes];
+                }
             } else {
 #pragma unroll
                 for (int i = 0; i < ITEMS; ++i) {
                     const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
                     const uint64_t gi = tbase + slot;
-                    keys[i] = slot < tvalidB ? src[reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
+                    const uint64_t si = reverse ? (n - 1u - gi) : gi;
+                    keys[i] = slot < tvalidB ? src[si] : KeyTraits<U>::fill();
+                    if constexpr (HAS_VAL) vals[i] = slot < tvalidB ? src_v[si] : 0ull;
                 }
             }
             R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, dmask);
@@ -849,13 +864,19 @@ __global__ void __launch_bounds__(THREADS, 2)
                     const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
                     const U k = stage[s];
                     const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
-                    if (uint64_t(g) < n) dst[g] = k;
+                    if (uint64_t(g) < n) {
+                        if (!HAS_VAL || dst) dst[g] = k;
+                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    }
                 }
             } else {
                 for (uint32_t s = tid; s < tvalidA; s += THREADS) {
                     const U k = stage[s];
                     const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
-                    if (uint64_t(g) < n) dst[g] = k;
+                    if (uint64_t(g) < n) {
+                        if (!HAS_VAL || dst) dst[g] = k;
+                        if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    }
                 }
             }
         }
@@ -866,7 +887,9 @@ __global__ void __launch_bounds__(THREADS, 2)
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalidB, pass, dmask);
-                stage[urow[d] + R::rank_of(rk, i)] = keys[i];
+                const uint32_t pos = urow[d] + R::rank_of(rk, i);
+                stage[pos] = keys[i];
+                if constexpr (HAS_VAL) stage_v[pos] = vals[i];
             }
             R::clear_own(utab);
         }

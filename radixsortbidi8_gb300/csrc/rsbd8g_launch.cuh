@@ -20,12 +20,12 @@ constexpr int kHistDirectThreads = 1024;  // direct keys: one CTA per SM
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch, uint32_t dmask,
                             cudaStream_t s) {
-    // direct keys: the pipelined pass, unless there are too few tiles to fill its pipeline (a sort
-    // of about one tile per CTA runs each tile's phases back to back in k_onesweep instead)
+    // the pipelined pass, unless there are too few tiles to fill its pipeline (a sort of about one
+    // tile per CTA runs each tile's phases back to back in k_onesweep instead)
     using SM = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
-    using PM = PipeSmem<U, THREADS, ITEMS>;
+    using PM = PipeSmem<U, THREADS, ITEMS, HAS_VAL>;
     auto kern = k_onesweep<U, MODE, HAS_VAL, THREADS, ITEMS, S>;
-    auto pkern = k_onesweep_pipe<U, MODE, THREADS, ITEMS, S>;
+    auto pkern = k_onesweep_pipe<U, MODE, HAS_VAL, THREADS, ITEMS, S>;
     int dev = 0;
     cudaGetDevice(&dev);
     static std::once_flag once[64];
@@ -36,16 +36,14 @@ cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsign
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, THREADS, SM::kBytes);
         occ[dev & 63] = b > 0 ? b : 1;
-        if constexpr (!HAS_VAL) {
-            cudaFuncSetAttribute(pkern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PM::kBytes));
-            cudaFuncSetAttribute(pkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-            int pb = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pkern, THREADS, PM::kBytes);
-            pocc[dev & 63] = pb > 0 ? pb : 1;
-        }
+        cudaFuncSetAttribute(pkern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(PM::kBytes));
+        cudaFuncSetAttribute(pkern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        int pb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, pkern, THREADS, PM::kBytes);
+        pocc[dev & 63] = pb > 0 ? pb : 1;
     });
-    const uint64_t resident = uint64_t(HAS_VAL ? occ[dev & 63] : pocc[dev & 63]) * device_sms(dev);
-    const bool pipe = !HAS_VAL && uint64_t(L.num_tiles) >= 2 * resident;
+    const uint64_t resident = uint64_t(pocc[dev & 63]) * device_sms(dev);
+    const bool pipe = uint64_t(L.num_tiles) >= 2 * resident;
     const uint32_t grid = uint32_t(std::min<uint64_t>(L.num_tiles, pipe ? resident : uint64_t(occ[dev & 63]) * device_sms(dev)));
     Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
     const unsigned long long *bstart = reinterpret_cast<const unsigned long long *>(scratch + L.bstart);

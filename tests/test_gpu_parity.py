@@ -399,3 +399,36 @@ def test_pipelined_pass_sixteen_byte_keys():
         y = torch.empty_like(x)
         assert rs.radixsortcopy(x, y, d, mode, key_dtype=kind)
         assert np.array_equal(y.cpu().numpy().view(np.uint64).reshape(-1, 2), O.sortcopy_wide(a, kind, mode, d)), kind
+
+
+@pytest.mark.parametrize("direction", DIRS)
+def test_pipelined_pass_pointer_payloads(direction):
+    """Indirect sorts with enough 4096-pointer tiles to run the pipelined pass (2.6 M objects: at
+    least two tiles per resident CTA), float64 keys in 24-byte records, against the oracle; and
+    uint32 keys at an unaligned offset of packed 13-byte objects, copy and in place."""
+    import torch
+    rs = R()
+    n = 2_600_017
+    rec = S.records24(0x5EED0021, n)
+    raw, base = _records_dev(rec)
+    ptrs = torch.arange(n, dtype=torch.int64, device="cuda") * 24 + base
+    out = torch.empty_like(ptrs)
+    assert rs.radixsortcopy_member(ptrs, out, np.float64, 8, direction)
+    idx = (out.cpu().numpy() - base) // 24
+    host_ptrs = np.uint64(rec.ctypes.data) + np.arange(n, dtype=np.uint64) * np.uint64(24)
+    want = (O.sortcopy_indirect(host_ptrs, np.float64, 8, "native", direction, threads=8)
+            - np.uint64(rec.ctypes.data)) // np.uint64(24)
+    assert np.array_equal(idx, want.astype(np.int64))
+    size, off = 13, 5
+    keys = mixed_input(np.uint32, n, 21)
+    obj = S.uniform_bits(41, n * size, np.uint8).reshape(n, size).copy()
+    obj[:, off:off + 4] = keys.view(np.uint8).reshape(n, 4)
+    odev = torch.from_numpy(obj.reshape(-1).copy()).cuda()
+    perm = np.argsort(S.splitmix64(5, n))
+    p = torch.from_numpy((perm * size).astype(np.int64)).cuda() + odev.data_ptr()
+    want_u = perm[O.numpy_sort_indices(keys[perm], "native", direction)]
+    o2 = torch.empty_like(p)
+    assert rs.radixsortcopy_member(p, o2, np.uint32, off, direction)
+    assert np.array_equal((o2.cpu().numpy() - odev.data_ptr()) // size, want_u)
+    assert rs.radixsort_member(p, np.uint32, off, direction)
+    assert np.array_equal((p.cpu().numpy() - odev.data_ptr()) // size, want_u)

@@ -80,12 +80,13 @@ def test_gpu_wide_pass_skip_and_inplace():
         assert np.array_equal(_host(x), O.sortcopy_wide(b, "x87", "native", d)), d
 
 
-def test_gpu_wide_member_indirection():
-    """32-byte records {u64 id; u64 pad; 16-byte key at byte 16}, sorted through object pointers."""
+@pytest.mark.parametrize("n", [50021, 1_900_003])
+def test_gpu_wide_member_indirection(n):
+    """32-byte records {u64 id; u64 pad; 16-byte key at byte 16}, sorted through object pointers
+    (1.9 M records: enough 3072-pointer tiles for the pipelined pass)."""
     import torch
     import radixsortbidi8_gb300 as rs
     from make_ref_wide import wide_input
-    n = 50021
     keys = wide_input("x87", n, 8)
     rec = np.zeros((n, 4), np.uint64)
     rec[:, 0] = np.arange(n, dtype=np.uint64)
