@@ -41,6 +41,8 @@ def _lib():
         L.rsbd8g_segmented_scratch_bytes.restype = ctypes.c_int
         L.rsbd8g_segmented_sortcopy.argtypes = [P, S, S, VP, VP, S, VP, VP, VP, ctypes.POINTER(SegTuning), VP]
         L.rsbd8g_segmented_sortcopy.restype = ctypes.c_int
+        L.rsbd8g_segmented_sortcopy_ptrs.argtypes = [P, S, S, VP, VP, VP, VP, VP, S, ctypes.POINTER(SegTuning), VP]
+        L.rsbd8g_segmented_sortcopy_ptrs.restype = ctypes.c_int
         L._seg_sigs = True
     return L
 
@@ -63,6 +65,30 @@ def segmented_scratch_bytes(key_dtype, total: int, nsegs: int, direction="ascfwd
     api._check(_lib().rsbd8g_segmented_scratch_bytes(ctypes.byref(d), total, nsegs, ctypes.byref(t),
                                                      ctypes.byref(out)), "rsbd8g_segmented_scratch_bytes")
     return out.value
+
+
+def segmented_sortcopy_ptrs(inputs, outputs, buffers, scratch, direction="ascfwdorder", mode="native",
+                            key_dtype=None, tuning: SegTuning | None = None, stream=None, flags: int = 0):
+    """Sort every device tensor of `inputs` into the tensor of `outputs` at the same place, using the
+    tensor of `buffers` there (rsbd8g_segmented_sortcopy_ptrs: one segment per array, in one call).
+    Stream-ordered; read device errors with api.scratch_status.  flags may carry
+    api.FLAG_DEVICE_ARRAYS when every array is device memory (tiles are then prefetched into L2).
+    Returns the device pointer tables and offsets: keep them until the call's work is done."""
+    import torch
+    dev = inputs[0].device
+    lens = [int(x.numel()) for x in inputs]
+    offs = torch.zeros(len(lens) + 1, dtype=torch.int64)
+    offs[1:] = torch.cumsum(torch.tensor(lens, dtype=torch.int64), 0)
+    tabs = [torch.tensor([api._ptr(x) if x.numel() else 0 for x in arrs], dtype=torch.int64).to(dev)
+            for arrs in (inputs, outputs, buffers)]
+    offs = offs.to(dev)
+    d = api.make_desc(key_dtype if key_dtype is not None else inputs[0].dtype, direction, mode, flags=flags)
+    t = tuning if tuning is not None else tuning_for(d.key_bytes)
+    api._check(_lib().rsbd8g_segmented_sortcopy_ptrs(
+        ctypes.byref(d), int(offs[-1]), len(lens), api._ptr(offs), api._ptr(tabs[0]), api._ptr(tabs[1]),
+        api._ptr(tabs[2]), api._ptr(scratch), scratch.numel() * scratch.element_size(), ctypes.byref(t),
+        api._stream(stream)), "rsbd8g_segmented_sortcopy_ptrs")
+    return tabs, offs
 
 
 def segmented_sortcopy(input, output, buffer, offsets, scratch, direction="ascfwdorder", mode="native",

@@ -133,3 +133,26 @@ def test_segmented_pipelined_pass_matches_oracle(dt, mode, direction):
     lens = rng_lens * 2
     a, offs = _segments(lens, dt, 31)
     _check(a, offs, dt, mode, direction)
+
+
+@pytest.mark.parametrize("flags", [0, 4])
+def test_segmented_pointer_tables_match_oracle(flags):
+    """The pointer-table form (one separate device array per segment) with and without
+    RSBD8G_FLAG_DEVICE_ARRAYS (= 4, which lets the pipelined pass prefetch tiles into L2), with
+    arrays enough for the pipelined pass, against the oracle per array."""
+    import torch
+    from radixsortbidi8_gb300 import api, batched as B
+    assert api.FLAG_DEVICE_ARRAYS == 4
+    lens = [1 << 20, 3, 700001, 0, 5000, (1 << 20) + 77, 12289, 1, 900007, 65536, 2 ** 19 + 5, 44444] * 2
+    arrays = [S.uniform_bits(101 + i, m, np.uint32) for i, m in enumerate(lens)]
+    ins = [to_dev(x) if x.size else torch.empty(0, dtype=torch.int32, device="cuda") for x in arrays]
+    outs = [torch.empty_like(x) for x in ins]
+    bufs = [torch.empty_like(x) for x in ins]
+    for direction in ("ascfwdorder", "dscrevorder"):
+        scratch = torch.empty(B.segmented_scratch_bytes(np.uint32, sum(lens), len(lens)), dtype=torch.uint8,
+                              device="cuda")
+        keep = B.segmented_sortcopy_ptrs(ins, outs, bufs, scratch, direction, key_dtype=np.uint32, flags=flags)
+        assert api.scratch_status(scratch) == 0
+        del keep
+        for x, o in zip(arrays, outs):
+            assert same_bits(from_dev(o, np.uint32), O.sortcopy(x, "native", direction)), x.size
