@@ -432,3 +432,46 @@ def test_pipelined_pass_pointer_payloads(direction):
     assert np.array_equal((o2.cpu().numpy() - odev.data_ptr()) // size, want_u)
     assert rs.radixsort_member(p, np.uint32, off, direction)
     assert np.array_equal((p.cpu().numpy() - odev.data_ptr()) // size, want_u)
+
+
+def _crowded(dt, n, seed):
+    """Keys whose digit 1 is 0x5A for about 70 % of them (a crowded pass: most lanes of a ranking
+    unit share one digit word) and uniform elsewhere, plus a run of equal keys."""
+    a = S.uniform_bits(seed, n, dt)
+    u = a.view(np.dtype(f"u{np.dtype(dt).itemsize}"))
+    pick = (S.splitmix64(seed + 1, n) % np.uint64(10)) < np.uint64(7)
+    u[pick] = (u[pick] & ~u.dtype.type(0xFF00)) | u.dtype.type(0x5A00)
+    a[n // 3:n // 3 + 5000] = a[7]
+    return a
+
+
+@pytest.mark.parametrize("dt,n", [(np.uint32, 100003), (np.uint32, (1 << 23) + 3), (np.int64, 70001),
+                                  (np.int64, (1 << 23) + 1), (np.float32, (1 << 23) + 5)])
+def test_crowded_pass_matches_oracle(dt, n):
+    """A pass whose histogram has a bucket with most of the keys: the plain and the pipelined scatter
+    pass, every direction, copy and in place."""
+    a = _crowded(dt, n, n % 977)
+    for d in DIRS:
+        want = O.sortcopy(a, "native", d, threads=8)
+        assert same_bits(gpu_copy(a, "native", d), want), d
+    assert same_bits(gpu_inplace(a, "native", "dscrevorder"), O.sortcopy(a, "native", "dscrevorder", threads=8))
+
+
+def test_crowded_pass_pointer_payloads():
+    """Warp ranking units under a crowded pass: an indirect sort whose float64 keys crowd one bucket
+    (75 % equal keys), at a size that runs the pipelined pass."""
+    import torch
+    rs = R()
+    n = 2_600_017
+    rec = S.records24(0x5EED0031, n)
+    k = rec["key"].copy()
+    pick = (S.splitmix64(9, n) % np.uint64(4)) != np.uint64(0)
+    k[pick] = 1.5                                  # 75 % equal keys: every digit crowded
+    rec["key"] = k
+    raw, base = _records_dev(rec)
+    ptrs = torch.arange(n, dtype=torch.int64, device="cuda") * 24 + base
+    for d in ("ascfwdorder", "dscrevorder"):
+        out = torch.empty_like(ptrs)
+        assert rs.radixsortcopy_member(ptrs, out, np.float64, 8, d)
+        idx = (out.cpu().numpy() - base) // 24
+        assert np.array_equal(idx, O.numpy_sort_indices(k, "native", d)), d

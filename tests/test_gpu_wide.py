@@ -113,3 +113,16 @@ def test_gpu_wide_argument_checks():
     offs = torch.tensor([0, 500, 1000], dtype=torch.int64, device="cuda")
     with pytest.raises(api.RSBD8GError):                   # no segmented form for 16-byte keys
         batched.segmented_scratch_bytes("u128", 1000, 2)
+
+
+def test_gpu_wide_crowded_pass():
+    """128-bit keys whose digit 1 is one value for ~70 % of them (warp ranking units under a crowded
+    pass), at a size that runs the pipelined pass."""
+    from make_ref_wide import wide_input
+    from radixsortbidi8_gb300 import synth as S
+    n = (1 << 21) + 13
+    a = wide_input("w128", n, 31)
+    pick = (S.splitmix64(17, n) % np.uint64(10)) < np.uint64(7)
+    a[pick, 0] = (a[pick, 0] & ~np.uint64(0xFF00)) | np.uint64(0x5A00)
+    for d in ("ascfwdorder", "dscrevorder"):
+        assert np.array_equal(_gpu_copy(a, "i128", "native", d), O.sortcopy_wide(a, "i128", "native", d)), d
