@@ -9,10 +9,13 @@
 //                                      pass-skip test, and the ping-pong plan of the passes
 //   k_onesweep                         one stable scatter pass of a surviving digit: persistent
 //                                      CTAs claim tiles in order, rank keys with a warp
-//                                      multisplit (shared-memory match words), resolve the tile's global
-//                                      bucket offsets with a bounded decoupled look-back, stage the
-//                                      tile in shared memory sorted by digit and write it out
-//                                      coalesced
+//                                      multisplit (TileRank: shared-memory match words), resolve
+//                                      the tile's global bucket offsets with a bounded decoupled
+//                                      look-back, stage the tile in shared memory sorted by digit
+//                                      and write it out coalesced
+//   k_onesweep_pipe                    the same pass with the look-back of one tile overlapping the
+//                                      load and ranking of the next, and the next tile prefetched
+//                                      into L2 (the pass of every sort of two tiles per CTA or more)
 //   k_copy                             the plain / reversed copy when parity or all-skipped
 //                                      passes need one
 #pragma once
@@ -523,7 +526,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
     long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
-    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..17] scan
+    uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..9] scan
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t *urow = R::row(wofs);
     const uint32_t tile = t.tile;
