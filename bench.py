@@ -284,7 +284,7 @@ def gb300_arm(args, rank: int, world: int):
     for r in recs:
         share[r["kernel"]] = share.get(r["kernel"], 0.0) + r["ms"]
     tot = sum(share.values())
-    roofline = {"bound": "hbm", "kernel": "k_onesweep<uint64> (int64 sort, 8 active passes)",
+    roofline = {"bound": "hbm", "kernel": "k_onesweep_pipe<uint64, 512 x 16> (int64 sort, 8 active passes)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": f"of {peak_kind}",
                 "traffic": profiled_traffic(), "bytes_per_launch": bytes_launch,
