@@ -169,10 +169,12 @@ rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r) {
 
 Layout layout_for(const Resolved &r, uint64_t n) {
     Layout L{};
-    const SweepGeometry g = sweep_geometry(int(r.key_bytes), r.indirect != 0);
+    L.wide_status = n >= kNarrowStatusLimit;
+    L.large_tiles = !r.indirect && r.key_bytes <= 4 && n >= kLargeTileMinKeys && !L.wide_status;
+    const SweepGeometry g = L.large_tiles ? sweep_geometry_large(int(r.key_bytes))
+                                          : sweep_geometry(int(r.key_bytes), r.indirect != 0);
     const int tile = g.threads * g.items;
     L.num_tiles = uint32_t((n + tile - 1) / tile);
-    L.wide_status = n >= kNarrowStatusLimit;
     const size_t sw = L.wide_status ? 8 : 4;
     const uint32_t passes = r.digits;
     L.ctrl = 0;

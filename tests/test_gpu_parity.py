@@ -475,3 +475,17 @@ def test_crowded_pass_pointer_payloads():
         assert rs.radixsortcopy_member(ptrs, out, np.float64, 8, d)
         idx = (out.cpu().numpy() - base) // 24
         assert np.array_equal(idx, O.numpy_sort_indices(k, "native", d)), d
+
+
+# counts from 2^25 up run keys of up to 4 bytes in 512 x 32 tiles
+LARGE_TILE_CASES = [(np.uint32, (1 << 25) + 7, "native", "dscrevorder"), (np.float32, 1 << 25, "nativeabs", "ascrevorder"),
+                    (np.int16, (1 << 25) + 3, "nativetieredabs", "dscfwdorder"), (np.uint8, (1 << 25) + 1, "native", "ascfwdorder"),
+                    (np.int32, (1 << 25) + 11, "native", "ascfwdorder")]
+
+
+@pytest.mark.parametrize("dt,n,mode,direction", LARGE_TILE_CASES, ids=lambda v: str(v))
+def test_large_tile_pass_matches_oracle(dt, n, mode, direction):
+    a = mixed_input(dt, n, n % 1013)
+    want = O.sortcopy(a, mode, direction, threads=8)
+    assert same_bits(gpu_copy(a, mode, direction), want)
+    assert same_bits(gpu_inplace(a, mode, direction), want)
