@@ -371,12 +371,13 @@ def test_lookback_timeout_in_the_pipelined_passes():
 
 
 # sizes that fill the pipelined scatter pass (at least two tiles per resident CTA on a 152-SM GB300:
-# 683 tiles of 12288 / 6144 / 3072 keys), every key size, filters, directions, in place
+# 683 tiles of 12288 keys up to 4 bytes, 1025 of 8192 8-byte keys), every key size, filters,
+# directions, in place
 PIPE_CASES = [(np.uint8, 1 << 23, "native", "ascrevorder"), (np.int16, (1 << 23) + 5, "nativeabs", "dscfwdorder"),
               (np.uint32, (1 << 23) + 7, "native", "dscrevorder"), (np.float32, (1 << 23) + 1, "nativeabs", "dscrevorder"),
               (np.float32, 1 << 23, "nativetieredabs", "ascrevorder"), (np.int32, 1 << 23, "nativetieredabs", "dscfwdorder"),
-              (np.int64, (1 << 22) + 3, "native", "ascfwdorder"), (np.float64, (1 << 22) + 9, "native", "dscrevorder"),
-              (np.uint64, 1 << 22, 4, "ascrevorder")]
+              (np.int64, (1 << 23) + 3, "native", "ascfwdorder"), (np.float64, (1 << 23) + 9, "native", "dscrevorder"),
+              (np.uint64, 1 << 23, 4, "ascrevorder")]
 
 
 @pytest.mark.parametrize("dt,n,mode,direction", PIPE_CASES, ids=lambda v: str(v))
