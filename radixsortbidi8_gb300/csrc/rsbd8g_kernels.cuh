@@ -403,10 +403,23 @@ struct TileRank {
         return run;
     }
 
-    // replace digit d's unit counts by the units' staging offsets, the first one at the tile start ts
-    __device__ static void offsets(uint32_t *tab, int d, uint32_t ts) {
+    // digit d's count over the units [U0, U1)
+    template <int U0, int U1>
+    __device__ static uint32_t total_of(const uint32_t *tab, int d) {
+        uint32_t run = 0;
 #pragma unroll
-        for (int u = 0; u < kUnits; ++u) {
+        for (int u = U0; u < U1; ++u) run += tab[u * kBuckets + d] >> kShift;
+        return run;
+    }
+
+    // replace digit d's unit counts by the units' staging offsets, the first one at the tile start ts
+    __device__ static void offsets(uint32_t *tab, int d, uint32_t ts) { offsets_of<0, kUnits>(tab, d, ts); }
+
+    // the same for the units [U0, U1), the first of them starting at ts
+    template <int U0, int U1>
+    __device__ static void offsets_of(uint32_t *tab, int d, uint32_t ts) {
+#pragma unroll
+        for (int u = U0; u < U1; ++u) {
             const uint32_t c = tab[u * kBuckets + d] >> kShift;
             tab[u * kBuckets + d] = ts;
             ts += c;
@@ -719,7 +732,8 @@ struct PipeSmem {
     static constexpr size_t kOffCnt = kOffTs + 2 * kBuckets * 4;      // u32 [2][256] tile counts
     static constexpr size_t kOffMisc = kOffCnt + 2 * kBuckets * 4;    // u32 [32]
     static constexpr size_t kOffAux = kOffMisc + 128;                 // 128 B for the kernel's own use
-    static constexpr size_t kBytes = kOffAux + 128;
+    static constexpr size_t kOffHalf = kOffAux + 128;                 // u32 [2][256]: split offset scan
+    static constexpr size_t kBytes = kOffHalf + 2 * kBuckets * 4;
 };
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
@@ -740,6 +754,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
     uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] next tile [1] bad [2..9] scan
+    // with 32 ranking units, all 512 threads write B's unit offsets in (3a), 16 units each: thread d
+    // the first half, thread d + 256 the second, from the digit's prefix and first-half count here
+    constexpr bool kSplit = R::kUnits == 32;
+    uint32_t *half = reinterpret_cast<uint32_t *>(smem + L::kOffHalf);
 
     const PassPlan plan = ctrl->plan[pass];
     if (!plan.active) return;
@@ -822,7 +840,13 @@ __global__ void __launch_bounds__(THREADS, 2)
         uint32_t x = 0, run = 0;
         if (tid < kBuckets) {
             if (hasB) {
-                run = R::total(utab, tid);
+                uint32_t h0 = 0;
+                if constexpr (kSplit) {
+                    h0 = R::template total_of<0, R::kUnits / 2>(utab, tid);
+                    run = h0 + R::template total_of<R::kUnits / 2, R::kUnits>(utab, tid);
+                } else {
+                    run = R::total(utab, tid);
+                }
                 uint32_t count = run;
                 if (tid == kBuckets - 1) count -= uint32_t(TILE) - tvalidB;      // the padding slots
                 cntB[tid] = count;
@@ -836,6 +860,10 @@ __global__ void __launch_bounds__(THREADS, 2)
                     if (lane >= o) x += y;
                 }
                 if (lane == 31) misc[2 + warp] = x;
+                if constexpr (kSplit) {
+                    half[tid] = x - run;              // the digit's prefix within its scan warp
+                    half[kBuckets + tid] = h0;
+                }
             }
         } else if (hasA) {
             const int d = tid - kBuckets;
@@ -852,8 +880,21 @@ __global__ void __launch_bounds__(THREADS, 2)
         }
         __syncthreads();                                                        // barrier 2
 
-        // ---- (3a) threads 0..255: B's tile starts and unit offsets; (3b) all: write A out
-        if (tid < kBuckets && hasB) {
+        // ---- (3a) B's tile starts and unit offsets; (3b) all: write A out
+        if constexpr (kSplit) {
+            if (hasB) {
+                const int d = tid & (kBuckets - 1);
+                uint32_t before = 0;
+                for (int i = 0; i < (d >> 5); ++i) before += misc[2 + i];
+                const uint32_t ts = before + half[d];
+                if (tid < kBuckets) {
+                    R::template offsets_of<0, R::kUnits / 2>(utab, d, ts);
+                    tsB[d] = ts;
+                } else {
+                    R::template offsets_of<R::kUnits / 2, R::kUnits>(utab, d, ts + half[kBuckets + d]);
+                }
+            }
+        } else if (tid < kBuckets && hasB) {
             uint32_t before = 0;
             for (int i = 0; i < warp; ++i) before += misc[2 + i];
             const uint32_t ts = before + x - run;
