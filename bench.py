@@ -292,6 +292,7 @@ def gb300_arm(args, rank: int, world: int):
                 "time_share": {k: round(v / tot, 4) for k, v in share.items() if tot}}
 
     extra = uniform_u32(args, rs, dev, stream, peak)
+    f32_rev = float32_abs_reverse(args, rs, arrays, stream)
     e2e = None if args.no_e2e else e2e_arm(args, rs, arrays, stream)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -303,6 +304,7 @@ def gb300_arm(args, rank: int, world: int):
         "data": "synthetic (seeded splitmix64; shapes and distributions of the benchmark configuration)",
         "config": workload_config(args.log2n),
         "roofline": roofline, "per_dtype": per_dtype, "uint32_uniform_2p28": extra,
+        "float32_abs_dscrevorder_2p28": f32_rev,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": len(ours), "checked": check,
     }
@@ -362,6 +364,34 @@ def uniform_u32(args, rs, dev, stream, peak) -> dict:
             "onesweep_avg_ms": round(sum(sw) / len(sw), 4),
             "onesweep_GBps": round(2 * 4 * n / (sum(sw) / len(sw) * 1e-3) / 1e9, 1),
             "histogram_ms": round(sum(hist) / len(hist), 4), "sorted": ok}
+
+
+def float32_abs_reverse(args, rs, arrays, stream) -> dict:
+    """The float32 array of the sweep sorted dscrevorder (descending by absolute value, ties in
+    reverse input order: the first surviving pass reads back to front), timed alone."""
+    import numpy as np
+    import torch
+    bits = arrays[0][1]
+    n = bits.numel()
+    out, buf = torch.empty_like(bits), torch.empty_like(bits)
+    scr = torch.empty(rs.scratch_bytes(np.float32, n, "dscrevorder", "nativeabs"), dtype=torch.uint8,
+                      device=bits.device)
+    run = lambda: rs.radixsortcopynoalloc(bits, out, buf, scr, "dscrevorder", "nativeabs", key_dtype=np.float32,
+                                          stream=stream)
+    for _ in range(max(3, args.warmup)):
+        run()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        run()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    k = out.to(torch.int64) & 0x7FFFFFFF          # |x| bits: the key of the absolute float modes
+    ok = bool((k[:-1] >= k[1:]).all())
+    del out, buf, scr
+    return {"gkeys_s": round(n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4), "sorted": ok}
 
 
 E2E_SLOTS = 2   # buffer sets of the end-to-end pipeline (three measured slower: 26.8 against 29.7 GKeys/s)
