@@ -436,6 +436,34 @@ struct TileRank {
     }
 };
 
+// ---- tile loads --------------------------------------------------------------------------------
+// This lane's ITEMS elements of a tile of `tile` slots: item i is slot slot0 + LANES * i, the
+// element tbase + slot of the array, or element n - 1 - (tbase + slot) when the pass reads back to
+// front; slots past tvalid (the array's end) get `fill`.  A full tile loads without checks, in
+// either direction.
+template <int ITEMS, int LANES, typename T>
+__device__ __forceinline__ void load_items(T (&v)[ITEMS], const T *src, uint64_t n, uint64_t tbase, uint32_t slot0,
+                                           uint32_t tvalid, uint32_t tile, bool reverse, T fill) {
+    if (tvalid == tile) {
+        if (!reverse) {
+            const T *p = src + tbase + slot0;
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) v[i] = p[size_t(i) * LANES];
+        } else {
+            const T *p = src + (n - 1u - tbase - slot0);
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) v[i] = *(p - size_t(i) * LANES);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t slot = slot0 + uint32_t(i) * LANES;
+            const uint64_t gi = tbase + slot;
+            v[i] = slot < tvalid ? src[reverse ? (n - 1u - gi) : gi] : fill;
+        }
+    }
+}
+
 // ---- tile prefetch ---------------------------------------------------------------------------------
 // Ask the L2 for elements [0, count) of p ahead of their loads: one bulk prefetch (the copy engine
 // fetches it while the SM works on the tile before), trimmed inward to 16-byte boundaries so it
@@ -553,26 +581,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     uint64_t vals[HAS_VAL ? ITEMS : 1];
     uint32_t rk[R::kRankRegs];
     const uint32_t slot0 = R::slot0();
-    if (!t.reverse && tvalid == TILE) {
-        const U *p = t.src_k + tbase + slot0;
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
-        if constexpr (HAS_VAL) {
-            const uint64_t *q = t.src_v + tbase + slot0;
-#pragma unroll
-            for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * R::kLanes];
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
-            const uint64_t gi = tbase + slot;
-            const uint64_t si = t.reverse ? (n - 1u - gi) : gi;
-            const bool ok = slot < tvalid;
-            keys[i] = ok ? t.src_k[si] : KeyTraits<U>::fill();
-            if constexpr (HAS_VAL) vals[i] = ok ? t.src_v[si] : 0ull;
-        }
-    }
+    load_items<ITEMS, R::kLanes>(keys, t.src_k, n, tbase, slot0, tvalid, TILE, t.reverse, KeyTraits<U>::fill());
+    if constexpr (HAS_VAL) load_items<ITEMS, R::kLanes>(vals, t.src_v, n, tbase, slot0, tvalid, TILE, t.reverse, uint64_t(0));
     R::template rank<MODE>(keys, rk, wofs, slot0, tvalid, pass, dmask);
     __syncthreads();
 
@@ -812,25 +822,8 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (hasB) {
             const uint64_t tbase = uint64_t(tileB) * TILE;
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
-            if (!reverse && tvalidB == TILE) {
-                const U *p = src + tbase + slot0;
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
-                if constexpr (HAS_VAL) {
-                    const uint64_t *q = src_v + tbase + slot0;
-#pragma unroll
-                    for (int i = 0; i < ITEMS; ++i) vals[i] = q[i * R::kLanes];
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
-                    const uint64_t gi = tbase + slot;
-                    const uint64_t si = reverse ? (n - 1u - gi) : gi;
-                    keys[i] = slot < tvalidB ? src[si] : KeyTraits<U>::fill();
-                    if constexpr (HAS_VAL) vals[i] = slot < tvalidB ? src_v[si] : 0ull;
-                }
-            }
+            load_items<ITEMS, R::kLanes>(keys, src, n, tbase, slot0, tvalidB, TILE, reverse, KeyTraits<U>::fill());
+            if constexpr (HAS_VAL) load_items<ITEMS, R::kLanes>(vals, src_v, n, tbase, slot0, tvalidB, TILE, reverse, uint64_t(0));
             R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, dmask);
         }
         __syncthreads();                                                        // barrier 1

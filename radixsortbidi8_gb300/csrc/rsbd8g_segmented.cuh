@@ -396,18 +396,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             const uint64_t n = B.n;
             const uint64_t tbase = uint64_t(B.tile) * TILE;
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
-            if (!B.reverse && tvalidB == TILE) {
-                const U *p = src + tbase + slot0;
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) keys[i] = p[i * R::kLanes];
-            } else {
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) {
-                    const uint32_t slot = slot0 + uint32_t(i) * R::kLanes;
-                    const uint64_t gi = tbase + slot;
-                    keys[i] = slot < tvalidB ? src[B.reverse ? (n - 1u - gi) : gi] : KeyTraits<U>::fill();
-                }
-            }
+            load_items<ITEMS, R::kLanes>(keys, src, n, tbase, slot0, tvalidB, TILE, B.reverse != 0, KeyTraits<U>::fill());
             R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, a.dmask);
         }
         __syncthreads();                                                        // barrier 1
