@@ -165,7 +165,7 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
  * The scratch and the ping-pong buffer live in one 64 MiB array in the library's device memory
  * (one per GPU, kept until the process exits), so `count` is limited to what fits there:
  * rsbd8g_scratch_bytes(count) + count * key_bytes rounded up to 256 bytes must not exceed
- * 64 MiB -- about 61.9 M one-byte, 30.9 M two-byte, 15.5 M four-byte or 7.45 M eight-byte
+ * 64 MiB -- about 63.1 M one-byte, 30.9 M two-byte, 15.5 M four-byte or 7.45 M eight-byte
  * keys.  Larger counts return RSBD8G_ERR_TOO_LARGE without touching the device.
  * The first call on a device looks up the array's device address (once per device), so make
  * that first call before capturing the stream into a CUDA graph.  Every call reuses the same

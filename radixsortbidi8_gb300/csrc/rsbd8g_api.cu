@@ -171,8 +171,10 @@ Layout layout_for(const Resolved &r, uint64_t n) {
     Layout L{};
     L.wide_status = n >= kNarrowStatusLimit;
     L.large_tiles = !r.indirect && r.key_bytes <= 4 && n >= kLargeTileMinKeys && !L.wide_status;
-    const SweepGeometry g = L.large_tiles ? sweep_geometry_large(int(r.key_bytes))
-                                          : sweep_geometry(int(r.key_bytes), r.indirect != 0);
+    L.small_tiles = !r.indirect && r.key_bytes <= 4 && n < kSmallTileMaxKeys;
+    const SweepGeometry g = L.large_tiles   ? sweep_geometry_large(int(r.key_bytes))
+                            : L.small_tiles ? sweep_geometry_small(int(r.key_bytes))
+                                            : sweep_geometry(int(r.key_bytes), r.indirect != 0);
     const int tile = g.threads * g.items;
     L.num_tiles = uint32_t((n + tile - 1) / tile);
     const size_t sw = L.wide_status ? 8 : 4;

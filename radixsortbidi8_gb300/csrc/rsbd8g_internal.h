@@ -31,6 +31,7 @@ struct Layout {
     uint32_t num_tiles;
     bool wide_status;
     bool large_tiles;     // sweep_geometry_large applies
+    bool small_tiles;     // sweep_geometry_small applies
 };
 
 // brackets one kernel launch with CUDA events on its stream while launch profiling is on
@@ -68,14 +69,19 @@ constexpr SweepGeometry sweep_geometry(int key_bytes, bool indirect) {
     if (indirect) return SweepGeometry{512, key_bytes == 16 ? 6 : 8};
     return SweepGeometry{512, key_bytes == 16 ? 6 : (key_bytes == 8 ? 16 : 24)};
 }
-// Direct keys of up to 4 bytes take tiles of 512 x 32 in sorts of at least kLargeTileMinKeys keys
-// (under 2^30, the narrow look-back words): fewer tiles mean fewer per-tile phases and shorter
-// look-back chains (uint32 2^28: -5 %).  Smaller sorts keep 512 x 24: larger tiles there leave SMs
-// without a tile or fall back to the unpipelined pass sooner (uint32 2^20: +10 %).  The choice
-// depends on the count alone, so a scratch size computed once fits every call of that count.
+// Direct keys of up to 4 bytes take three tile sizes by the count of the sort (narrow look-back
+// words only, under 2^30 keys): 512 x 32 from kLargeTileMinKeys keys on -- fewer tiles mean fewer
+// per-tile phases and shorter look-back chains (uint32 2^28: -5 % against 512 x 24) -- 512 x 24 in
+// between, and 512 x 16 below kSmallTileMaxKeys, where more tiles keep every SM busy and fill the
+// pipelined pass sooner (uint32 2^20 / 2^21 / 2^22: -10 / -10 / -5 %).  The choice depends on the
+// count alone, so a scratch size computed once fits every call of that count.
 constexpr uint64_t kLargeTileMinKeys = uint64_t(1) << 25;
+constexpr uint64_t kSmallTileMaxKeys = uint64_t(1) << 23;
 constexpr SweepGeometry sweep_geometry_large(int key_bytes) {
     return key_bytes <= 4 ? SweepGeometry{512, 32} : sweep_geometry(key_bytes, false);
+}
+constexpr SweepGeometry sweep_geometry_small(int key_bytes) {
+    return key_bytes <= 4 ? SweepGeometry{512, 16} : sweep_geometry(key_bytes, false);
 }
 // the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
 // segment's last tile is partly empty, and large 8-byte segments are the shorter ones)

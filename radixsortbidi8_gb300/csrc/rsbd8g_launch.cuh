@@ -91,6 +91,7 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
                           void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s) {
     constexpr SweepGeometry gd = sweep_geometry(int(sizeof(U)), false);
     constexpr SweepGeometry gl = sweep_geometry_large(int(sizeof(U)));
+    constexpr SweepGeometry gs = sweep_geometry_small(int(sizeof(U)));
     constexpr SweepGeometry gi = sweep_geometry(int(sizeof(U)), true);
     cudaError_t e;
     {
@@ -138,6 +139,10 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
 #undef RSBD8G_SWEEP
     } else if (L.large_tiles) {
 #define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gl.threads, gl.items, uint32_t>(P, n, L, scratch, dmask, s)
+        RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
+#undef RSBD8G_SWEEP
+    } else if (L.small_tiles) {
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gs.threads, gs.items, uint32_t>(P, n, L, scratch, dmask, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else {

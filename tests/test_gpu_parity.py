@@ -377,7 +377,9 @@ PIPE_CASES = [(np.uint8, 1 << 23, "native", "ascrevorder"), (np.int16, (1 << 23)
               (np.uint32, (1 << 23) + 7, "native", "dscrevorder"), (np.float32, (1 << 23) + 1, "nativeabs", "dscrevorder"),
               (np.float32, 1 << 23, "nativetieredabs", "ascrevorder"), (np.int32, 1 << 23, "nativetieredabs", "dscfwdorder"),
               (np.int64, (1 << 23) + 3, "native", "ascfwdorder"), (np.float64, (1 << 23) + 9, "native", "dscrevorder"),
-              (np.uint64, 1 << 23, 4, "ascrevorder")]
+              (np.uint64, 1 << 23, 4, "ascrevorder"),
+              # the 512 x 16 tiles of keys up to 4 bytes below 2^23 keys, pipelined from 608 tiles on
+              (np.uint32, 6_000_011, "native", "ascrevorder"), (np.float32, (3 << 21) + 9, "nativeabs", "dscfwdorder")]
 
 
 @pytest.mark.parametrize("dt,n,mode,direction", PIPE_CASES, ids=lambda v: str(v))
