@@ -96,3 +96,19 @@ def test_sixteen_byte_key_descriptors():
     for kb, kind in ((8, api.KIND_X87), (2, api.KIND_X87), (12, api.KIND_UNSIGNED), (16, 4)):
         d = api.Desc(kb, kind, 64, 0, 0, 0, 0, 0)
         assert L.rsbd8g_scratch_bytes(ctypes.byref(d), 1000, ctypes.byref(out)) == api.ERR_BAD_ARG, (kb, kind)
+
+
+def test_tile_tiers_follow_the_count():
+    """Keys of up to 4 bytes take 512 x 16 tiles below 2^23 keys, 512 x 24 up to 2^25 and 512 x 32
+    from there on; the scratch size (look-back words: one per tile, digit pass and bucket) shows it."""
+    kib = 1024
+    for dt, passes in ((np.uint32, 4), (np.uint16, 2)):
+        for n, tile in (((1 << 23) - 1, 8192), (1 << 23, 12288), ((1 << 25) - 1, 12288), (1 << 25, 16384)):
+            tiles = -(-n // tile)
+            body = tiles * passes * kib               # 256 buckets x 4 bytes per tile and pass
+            s = rs.scratch_bytes(dt, n)
+            assert body <= s < body + 128 * kib, (dt, n, s, body)
+    # 8-byte keys keep 512 x 16 at every count below 2^30
+    for n in ((1 << 23) - 1, 1 << 25):
+        body = -(-n // 8192) * 8 * kib
+        assert body <= rs.scratch_bytes(np.int64, n) < body + 128 * kib
