@@ -171,9 +171,19 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
  * that first call before capturing the stream into a CUDA graph.  Every call reuses the same
  * array and clears the parts that must start at zero; calls whose work overlaps on the GPU
  * (other streams, other host threads) race on it, so order them.  Stream-ordered like the
- * noalloc forms: read errors with a synchronising call of your own. */
+ * noalloc forms: the return value only says whether the work was enqueued.  A failure on the
+ * device (a bounded wait that ran out) sets a status word inside the array and leaves the
+ * output undefined; no CUDA error reports it, so a stream synchronisation alone does not see
+ * it -- read it with rsbd8g_static_status before the next call on the device clears it. */
 RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_static(const rsbd8g_desc *desc, size_t count,
                                                      const void *input, void *output, rsbd8g_stream stream);
+
+/* Wait for `stream`, then read and clear the device-side status word that the last
+ * rsbd8g_radixsortcopy_static call on the current device left in the library's array:
+ * RSBD8G_OK, RSBD8G_ERR_TIMEOUT (a bounded device-side wait ran out; that call's output is
+ * undefined) or RSBD8G_ERR_DEVICE_FAULT.  Pass the stream the sort was enqueued on.  Allocates
+ * nothing.  No counterpart in the reference (its functions report no device state). */
+RSBD8G_API rsbd8g_status rsbd8g_static_status(rsbd8g_stream stream);
 
 /* ---- batched (segmented) sort -------------------------------------------------------------
  * Many independent arrays of uneven sizes in one stream-ordered call: segment s is elements
@@ -278,6 +288,11 @@ RSBD8G_API rsbd8g_status rsbd8g_profile_collect(rsbd8g_launch_record *records, s
 
 /* Library version: major * 10000 + minor * 100 + patch. */
 RSBD8G_API int rsbd8g_version(void);
+
+/* The architecture the library's kernels were compiled for, as the CUDA runtime reports it for
+ * the loaded module on the current device (cudaFuncAttributes::binaryVersion: 103 for sm_103a).
+ * Needs a device.  No counterpart in the reference. */
+RSBD8G_API rsbd8g_status rsbd8g_binary_version(int *version);
 
 #ifdef __cplusplus
 }

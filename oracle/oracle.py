@@ -104,6 +104,8 @@ def lib():
         L.rsbd8o_skipmask.argtypes = [ctypes.POINTER(Desc), ctypes.c_uint64, ctypes.c_void_p,
                                       ctypes.c_uint32]
         L.rsbd8o_skipmask.restype = ctypes.c_uint32
+        L.rsbd8o_sortcopy_batch.argtypes = [ctypes.c_uint64, ctypes.POINTER(Job), ctypes.c_uint]
+        L.rsbd8o_sortcopy_batch.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -141,6 +143,53 @@ def sortcopy_indirect(ptrs: np.ndarray, key_dtype, offset1: int, mode="native",
     rc = lib().rsbd8o_sortcopy(ctypes.byref(d), ptrs.size, ptrs.ctypes.data, out.ctypes.data, threads)
     if rc != 0:
         raise RuntimeError(f"oracle sort failed ({rc})")
+    return out
+
+
+class Job(ctypes.Structure):
+    """rsbd8o_job of rsbd8_oracle.h"""
+    _fields_ = [("d", ctypes.POINTER(Desc)), ("n", ctypes.c_uint64), ("inp", ctypes.c_void_p),
+                ("out", ctypes.c_void_p)]
+
+
+def sortcopy_batch(items, threads: int = 1) -> list:
+    """Independent stable sorts, `threads` at a time: items are (array, mode, direction);
+    returns the sorted arrays (the reference's callers loop over radixsortcopy per array)."""
+    arrays = [np.ascontiguousarray(a) for a, _, _ in items]
+    outs = [np.empty_like(a) for a in arrays]
+    descs = [resolve(a.dtype, m, d) for a, (_, m, d) in zip(arrays, items)]
+    jobs = (Job * max(1, len(arrays)))()
+    for i, (a, o, d) in enumerate(zip(arrays, outs, descs)):
+        jobs[i].d = ctypes.pointer(d)
+        jobs[i].n = a.size
+        jobs[i].inp = a.ctypes.data
+        jobs[i].out = o.ctypes.data
+    rc = lib().rsbd8o_sortcopy_batch(len(arrays), jobs, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle batch sort failed ({rc})")
+    return outs
+
+
+def sortcopy_segments(a: np.ndarray, offsets: np.ndarray, mode="native", direction="ascfwdorder",
+                      threads: int = 1) -> np.ndarray:
+    """Every segment [offsets[s], offsets[s+1]) of `a` sorted on its own, as one
+    rsbd8::radixsortcopy per segment; returns the concatenated result."""
+    a = np.ascontiguousarray(a)
+    out = np.empty_like(a)
+    d = resolve(a.dtype, mode, direction)
+    offs = np.asarray(offsets, dtype=np.int64)
+    nseg = offs.size - 1
+    jobs = (Job * max(1, nseg))()
+    dp = ctypes.pointer(d)
+    es = a.dtype.itemsize
+    for s in range(nseg):
+        jobs[s].d = dp
+        jobs[s].n = int(offs[s + 1] - offs[s])
+        jobs[s].inp = a.ctypes.data + int(offs[s]) * es
+        jobs[s].out = out.ctypes.data + int(offs[s]) * es
+    rc = lib().rsbd8o_sortcopy_batch(nseg, jobs, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle segmented sort failed ({rc})")
     return out
 
 

@@ -279,6 +279,56 @@ int rsbd8o_sortcopy(const rsbd8o_desc *d, uint64_t n, const void *in, void *out,
     return 0;
 }
 
+/* ---- batches of independent sorts ------------------------------------- */
+/* The reference has no batched entry point: its callers loop over radixsortcopy per array
+ * (Radixsortbidi8.hpp:60476).  The oracle runs that loop with one sort per worker thread,
+ * the workers taking the next job from a shared counter. */
+
+typedef struct batchctl {
+    uint64_t njobs;
+    const rsbd8o_job *jobs;
+    uint64_t next;          /* next job to take (guarded by mu) */
+    int rc;
+    pthread_mutex_t mu;
+} batchctl;
+
+static void *batch_work(void *arg)
+{
+    batchctl *b = (batchctl *)arg;
+    for (;;) {
+        pthread_mutex_lock(&b->mu);
+        const uint64_t i = b->next++;
+        pthread_mutex_unlock(&b->mu);
+        if (i >= b->njobs) break;
+        const rsbd8o_job *jb = &b->jobs[i];
+        int rc = rsbd8o_sortcopy(jb->d, jb->n, jb->in, jb->out, 1);
+        if (rc != 0) {
+            pthread_mutex_lock(&b->mu);
+            if (b->rc == 0) b->rc = rc;
+            pthread_mutex_unlock(&b->mu);
+        }
+    }
+    return NULL;
+}
+
+int rsbd8o_sortcopy_batch(uint64_t njobs, const rsbd8o_job *jobs, unsigned threads)
+{
+    if (njobs == 0) return 0;
+    if (threads == 0) threads = 1;
+    if (threads > 256) threads = 256;
+    if ((uint64_t)threads > njobs) threads = (unsigned)njobs;
+    batchctl b;
+    b.njobs = njobs; b.jobs = jobs; b.next = 0; b.rc = 0;
+    pthread_mutex_init(&b.mu, NULL);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    for (unsigned t = 1; t < threads; ++t) pthread_create(&th[t], NULL, batch_work, &b);
+    batch_work(&b);
+    for (unsigned t = 1; t < threads; ++t) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&b.mu);
+    free(th);
+    return b.rc;
+}
+
 /* which digits the reference's pass-skip test would drop (bit g = digit g) */
 uint32_t rsbd8o_skipmask(const rsbd8o_desc *d, uint64_t n, const void *in, uint32_t digit_bits_override)
 {

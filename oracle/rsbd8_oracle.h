@@ -31,6 +31,16 @@ int rsbd8o_resolve(uint32_t kind, uint32_t mode, uint32_t direction, uint32_t in
 uint64_t rsbd8o_sortkey(uint64_t bits, uint32_t key_bytes, const rsbd8o_desc *d);
 /* stable sort of n elements from in to out (keys, or 8-byte pointers when indirect) */
 int rsbd8o_sortcopy(const rsbd8o_desc *d, uint64_t n, const void *in, void *out, unsigned threads);
+/* many independent sorts (segments of a batch, requests of a serving run): job i sorts
+ * jobs[i].n elements from jobs[i].in to jobs[i].out under *jobs[i].d, each single-threaded,
+ * `threads` jobs at a time; returns 0, or the first failing job's code */
+typedef struct rsbd8o_job {
+    const rsbd8o_desc *d;
+    uint64_t n;
+    const void *in;
+    void *out;
+} rsbd8o_job;
+int rsbd8o_sortcopy_batch(uint64_t njobs, const rsbd8o_job *jobs, unsigned threads);
 /* bit g set when digit g (of digit_bits, 0 = the reference's own width) is skipped */
 uint32_t rsbd8o_skipmask(const rsbd8o_desc *d, uint64_t n, const void *in, uint32_t digit_bits);
 

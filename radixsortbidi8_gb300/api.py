@@ -97,6 +97,9 @@ def lib():
         "rsbd8g_version": ([], I32),
         "rsbd8g_profile_enable": ([I32], I32),
         "rsbd8g_profile_collect": ([ctypes.POINTER(LaunchRecord), S, ctypes.POINTER(ctypes.c_size_t)], I32),
+        "rsbd8g_radixsortcopy_static": ([P, S, VP, VP, VP], I32),
+        "rsbd8g_static_status": ([VP], I32),
+        "rsbd8g_binary_version": ([ctypes.POINTER(I32)], I32),
     }
     for name, (args, res) in sigs.items():
         f = getattr(L, name)
@@ -258,6 +261,14 @@ def radixsortnoalloc(input, buffer, scratch, movetobuffer: bool = False, directi
 def scratch_status(scratch, stream=None) -> int:
     """Wait for the stream and read (and clear) the device status word of a scratch area."""
     return int(lib().rsbd8g_scratch_status(_ptr(scratch), _stream(stream)))
+
+
+def binary_version() -> int:
+    """The architecture the loaded kernels were compiled for, as the CUDA runtime reports it
+    (103 for sm_103a); needs a device."""
+    v = ctypes.c_int(0)
+    _check(lib().rsbd8g_binary_version(ctypes.byref(v)), "rsbd8g_binary_version")
+    return v.value
 
 
 # ---- indirection --------------------------------------------------------------------------

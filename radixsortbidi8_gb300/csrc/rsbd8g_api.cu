@@ -251,13 +251,28 @@ rsbd8g_status read_device_status(void *scratch, cudaStream_t s, bool clear) {
 
 }  // namespace rsbd8g
 
+// an empty kernel of this library's module: its attributes give the architecture the module was
+// compiled for (cudaFuncAttributes::binaryVersion)
+static __global__ void k_binary_probe() {}
+
 // ---- the C ABI --------------------------------------------------------------------------------
 
 using namespace rsbd8g;
 
 extern "C" {
 
-RSBD8G_API int rsbd8g_version(void) { return 100; }
+RSBD8G_API int rsbd8g_version(void) { return 200; }
+
+RSBD8G_API rsbd8g_status rsbd8g_binary_version(int *version) {
+    if (!version) return RSBD8G_ERR_BAD_ARG;
+    cudaFuncAttributes at{};
+    if (cudaFuncGetAttributes(&at, k_binary_probe) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return RSBD8G_ERR_CUDA;
+    }
+    *version = at.binaryVersion;
+    return RSBD8G_OK;
+}
 
 RSBD8G_API rsbd8g_status rsbd8g_profile_enable(int enable) { return profile_enable(enable); }
 

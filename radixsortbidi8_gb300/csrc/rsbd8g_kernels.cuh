@@ -648,6 +648,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
                 if (uint64_t(g) < n) {
                     if (t.dst_k) t.dst_k[g] = k;
                     if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
+                } else {
+                    atomicOr(err_word, kDevFault);      // an offset outside the array: flagged, not written
                 }
             }
         } else {
@@ -657,6 +659,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
                 if (uint64_t(g) < n) {
                     if (t.dst_k) t.dst_k[g] = k;
                     if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
+                } else {
+                    atomicOr(err_word, kDevFault);      // an offset outside the array: flagged, not written
                 }
             }
         }
@@ -904,6 +908,8 @@ __global__ void __launch_bounds__(THREADS, 2)
                     if (uint64_t(g) < n) {
                         if (!HAS_VAL || dst) dst[g] = k;
                         if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    } else {
+                        atomicOr(err_word, kDevFault);  // an offset outside the array: flagged, not written
                     }
                 }
             } else {
@@ -913,6 +919,8 @@ __global__ void __launch_bounds__(THREADS, 2)
                     if (uint64_t(g) < n) {
                         if (!HAS_VAL || dst) dst[g] = k;
                         if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
+                    } else {
+                        atomicOr(err_word, kDevFault);  // an offset outside the array: flagged, not written
                     }
                 }
             }

@@ -449,6 +449,7 @@ __global__ void __launch_bounds__(THREADS, 2)
                 const U k = stage[s];
                 const long long g = gofs[pass_digit<MODE>(k, pass, a.dmask)] + (long long)s;
                 if (uint64_t(g) < n) dst[g] = k;
+                else atomicOr(err_word, kDevFault);     // an offset outside the segment: flagged, not written
             }
         }
         __syncthreads();                                                        // barrier 3

@@ -192,3 +192,129 @@ def float_specials_torch(seed: int, n: int, key_bytes: int = 4, sigma: float = 1
     bits[(r > 0.015) & (r <= 0.0155)] = qnan
     bits[(r > 0.0155) & (r <= 0.016)] = nqnan
     return bits
+
+
+def unit_interval_torch(z):
+    """unit_interval() of a splitmix64_torch stream: float64 in (0, 1], the same values."""
+    import torch
+    return (((z >> 11) & ((1 << 53) - 1)).to(torch.float64) + 1.0) * (1.0 / 9007199254740992.0)
+
+
+def normal_torch(seed: int, n: int, stream: int = 0, device="cuda"):
+    """normal() on the device: the same Irwin-Hall sum in the same order, so the same bits."""
+    import torch
+    acc = torch.zeros(n, dtype=torch.float64, device=device)
+    for k in range(12):
+        acc += unit_interval_torch(splitmix64_torch(seed, n, device, stream=100 * stream + k + 1))
+    return acc - 6.0
+
+
+def exp2_det_torch(t):
+    """exp2_det() on the device: the same Taylor polynomial, and 2**i built from its exponent bits
+    (exact), so the same bits."""
+    import torch
+    i = torch.floor(t)
+    x = (t - i) * 0.6931471805599453
+    p = torch.ones_like(x)
+    term = torch.ones_like(x)
+    for k in range(1, 12):
+        term = term * x / float(k)
+        p = p + term
+    scale = ((i.to(torch.int64) + 1023) << 52).view(torch.float64)
+    return p * scale
+
+
+def records24_torch(seed: int, n: int, device="cuda"):
+    """records24() built on the device, bit for bit: an (n, 3) int64 tensor holding the n 24-byte
+    records {u64 id, f64 key, u32 tag, u32 pad = 0}, row i at byte 24 * i."""
+    import torch
+    ar = torch.arange(n, dtype=torch.int64, device=device)
+    key = exp2_det_torch(normal_torch(seed, n, device=device) * (2.0 / 0.6931471805599453))
+    sgn = (splitmix64_torch(seed, n, device, stream=11) & 1).bool()
+    key = torch.where(sgn, -key, key)
+    dup = unit_interval_torch(splitmix64_torch(seed, n, device, stream=12)) <= 0.1
+    dup[0] = False
+    src = (unit_interval_torch(splitmix64_torch(seed, n, device, stream=13)) * ar.to(torch.float64)).to(torch.int64)
+    src = torch.minimum(src, torch.clamp(ar - 1, min=0))
+    root = torch.where(dup, src, ar)
+    while True:
+        chain = dup[root]
+        if not bool(chain.any()):
+            break
+        root[chain] = src[root[chain]]
+    rec = torch.empty((n, 3), dtype=torch.int64, device=device)
+    rec[:, 0] = ar
+    rec[:, 1] = key[root].view(torch.int64)
+    rec[:, 2] = splitmix64_torch(seed, n, device, stream=14) & 0xFFFFFFFF
+    return rec
+
+
+# ---- the benchmark configurations' inputs ------------------------------------------------
+
+# seeds of the mode/dtype sweep (three arrays of one size) and of the uniform uint32 array
+SWEEP_SEEDS = {"f32": 0x5EED0002, "i64": 0x5EED0003, "u32low12": 0x5EED0004, "u32": 0x5EED0005}
+RECORDS_SEED = 0x5EED0003
+BATCH_A_SEED, BATCH_B_SEED, SERVING_SEED = 0x5EED0005, 0x5EED0006, 0x5EED0007
+
+
+def sweep_arrays_torch(n: int, device="cuda"):
+    """The mode/dtype sweep, one array each of n keys, on the device:
+    (name, key bits tensor, key dtype, direction, mode) for float32 N(0, 1e3) with specials sorted
+    descending with the absolute filter, int64 uniform ascending, and uint32 with only the low 12
+    bits random ascending."""
+    return [
+        ("float32_abs_dscfwdorder", float_specials_torch(SWEEP_SEEDS["f32"], n, 4, device=device), np.float32,
+         "dscfwdorder", "nativeabs"),
+        ("int64_ascfwdorder", uniform_bits_torch(SWEEP_SEEDS["i64"], n, 8, device=device), np.int64,
+         "ascfwdorder", "native"),
+        ("uint32_low12_ascfwdorder", low_bits_u32_torch(SWEEP_SEEDS["u32low12"], n, device=device), np.uint32,
+         "ascfwdorder", "native"),
+    ]
+
+
+def batch_lengths(which: str, scale: float = 1.0) -> np.ndarray:
+    """Segment lengths of the batched configuration: "A" 100,000 uint32 arrays log-uniform in
+    [16, 2^20]; "A_2p28" the same list cut where the running total reaches 2^28 keys; "B" 20,000
+    float64 arrays log-uniform in [64, 2^18]."""
+    if which in ("A", "A_2p28"):
+        lens = log_uniform_lengths(BATCH_A_SEED, max(1, int(100000 * scale)), 16, 1 << 20)
+        if which == "A_2p28":
+            cut = int(np.searchsorted(np.cumsum(lens), 1 << 28))
+            lens = lens[:max(1, cut)]
+        return lens
+    if which == "B":
+        return log_uniform_lengths(BATCH_B_SEED, max(1, int(20000 * scale)), 64, 1 << 18)
+    raise ValueError(which)
+
+
+def batch_keys_torch(which: str, total: int, device="cuda"):
+    """Concatenated keys of a batch (uint32 uniform bits for A, float64 with specials for B), built
+    in chunks of 2^27 keys on the device."""
+    import torch
+    key_bytes = 4 if which.startswith("A") else 8
+    seed = BATCH_A_SEED if key_bytes == 4 else BATCH_B_SEED
+    t = torch.int32 if key_bytes == 4 else torch.int64
+    keys = torch.empty(total, dtype=t, device=device)
+    chunk = 1 << 27
+    for o in range(0, total, chunk):
+        m = min(chunk, total - o)
+        keys[o:o + m] = uniform_bits_torch(seed + o, m, 4, device=device) if key_bytes == 4 else \
+            float_specials_torch(seed + o, m, 8, device=device)
+    return keys
+
+
+SERVING_KINDS = (np.uint16, np.int32, np.float32, np.float64)
+
+
+def serving_requests(rate: float, duration: float, lo: int = 1 << 10, hi: int = 1 << 26):
+    """The serving configuration's request stream: arrival times (Poisson at `rate` per second for
+    `duration` seconds), lengths log-uniform in [lo, hi], key type uniform over SERVING_KINDS,
+    direction ascending/descending (forward order) and the absolute filter each with
+    probability 1/2.  Returns (arrivals, lengths, kind index, descending flag, abs flag)."""
+    arr = poisson_arrivals(SERVING_SEED, rate, duration)
+    nreq = arr.size
+    lens = log_uniform_lengths(SERVING_SEED, nreq, lo, hi)
+    kind = (splitmix64(SERVING_SEED, nreq, stream=41) % np.uint64(len(SERVING_KINDS))).astype(int)
+    desc = (splitmix64(SERVING_SEED, nreq, stream=42) & np.uint64(1)).astype(int)
+    absf = (splitmix64(SERVING_SEED, nreq, stream=43) & np.uint64(1)).astype(int)
+    return arr, lens, kind, desc, absf
