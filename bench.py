@@ -55,7 +55,10 @@ def parse_args():
     p.add_argument("--log2n", type=int, default=28, help="keys per array (2^log2n)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind", "u128", "x87"],
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the other benchmark configurations (2^20 plain sort, records, batches, serving)")
+    p.add_argument("--case", default=None, choices=["u32", "i64", "f32abs", "u32low12", "f64ind", "u128", "x87",
+                                                    "merge_u32", "merge_i64"],
                    help="profiling aid: sort only this one array --steps times and print its timings")
     p.add_argument("--config", default="sweep", choices=["sweep", "batched", "serving"],
                    help="sweep: the default line; batched: segmented batches vs a per-array loop; "
@@ -289,6 +292,17 @@ def gb300_arm(args, rank: int, world: int):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(arrays, min(args.log2n, 24))
+    # the other benchmark configurations, each timed on its own and checked against the oracle
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        del bufs
+        torch.cuda.empty_cache()
+        do_check = not args.no_cpu
+        configs = {"1_plain_u32_2p20": config1_small(args, rs, dev, stream),
+                   "3_records_2p26": config3_records(args, rs, dev, stream, peak),
+                   "4_batched": {w: batched_run(args, w, max(3, min(args.steps, 10)), do_check)
+                                 for w in ("A_2p28", "B")},
+                   "5_serving": serving_run(args, 2000.0, 5.0, 2000, 32 if do_check else 0)}
     line = {
         "metric": "GKeys/s", "value": round(value, 3), "unit": "GKeys/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
@@ -298,7 +312,7 @@ def gb300_arm(args, rank: int, world: int):
         "roofline": roofline, "per_dtype": per_dtype, "uint32_uniform_2p28": extra,
         "float32_abs_dscrevorder_2p28": f32_rev,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-        "gpu_launches": len(ours), "checked": check,
+        "gpu_launches": len(ours), "checked": check, "configs": configs,
     }
     return line
 
@@ -468,6 +482,31 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
         return t0.elapsed_time(t1) / steps
 
     ms_serial = timed(False)
+
+    def stages() -> dict:
+        """One serial step with CUDA events between its stages: where an end-to-end step spends its time."""
+        slot = slots[0]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * len(arrays) + 1)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for i, (nm, b, kdt, d, m) in enumerate(arrays):
+                slot["in"][i].copy_(host_in[i], non_blocking=True)
+                ev[3 * i + 1].record(stream)
+                rs.radixsortcopynoalloc(slot["in"][i], slot["out"][i], slot["buf"][i], slot["scr"][i], d, m,
+                                        key_dtype=kdt, stream=stream)
+                ev[3 * i + 2].record(stream)
+                slot["host_out"][i].copy_(slot["out"][i], non_blocking=True)
+                ev[3 * i + 3].record(stream)
+        torch.cuda.synchronize()
+        out = {}
+        for i, (nm, *_) in enumerate(arrays):
+            out[nm] = {"h2d_ms": round(ev[3 * i].elapsed_time(ev[3 * i + 1]), 3),
+                       "sort_ms": round(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]), 3),
+                       "d2h_ms": round(ev[3 * i + 2].elapsed_time(ev[3 * i + 3]), 3)}
+        return out
+
+    stage_ms = stages()
     # the host link is shared with the machine's other GPUs: three pipelined runs, the median kept
     runs = sorted(timed(True) for _ in range(3))
     ms = runs[1]
@@ -505,6 +544,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
             "serial": {"value": round(3 * n / (ms_serial * 1e-3) / 1e9, 3), "ms_per_step": round(ms_serial, 3),
                        "path": "the same calls in order on one stream"},
             "runs_ms_per_step": [round(r, 3) for r in runs], "host_results_match_device": bool(same),
+            "serial_stage_ms": stage_ms,
             "copy_bandwidth": copies}
 
 
@@ -575,7 +615,18 @@ def single_case(args) -> dict:
     dev = torch.device("cuda", 0)
     n = 1 << args.log2n
     stream = torch.cuda.current_stream()
-    if args.case == "f64ind":
+    if args.case in ("merge_u32", "merge_i64"):
+        # the two halves of a uniform array, each sorted, merged into one (the reference's mergehalves*)
+        kb = 4 if args.case == "merge_u32" else 8
+        kdt = np.uint32 if kb == 4 else np.int64
+        bits = S.uniform_bits_torch(SEEDS["u32"] if kb == 4 else SEEDS["i64"], n, kb, device=dev)
+        runs = torch.empty_like(bits)
+        h = rs.api.halves(n)
+        rs.radixsortcopy(bits[:h[0]], runs[:h[0]], key_dtype=kdt)
+        rs.radixsortcopy(bits[h[0]:], runs[h[0]:], key_dtype=kdt)
+        out = torch.empty_like(bits)
+        run = lambda: rs.api.merge_runs(runs, out, h, key_dtype=kdt, stream=stream)
+    elif args.case == "f64ind":
         rec = torch.empty(n * 24, dtype=torch.uint8, device=dev)
         keys = S.float_specials_torch(SEEDS["f32"], n, 8, device=dev)
         rec.view(torch.int64).view(n, 3)[:, 1] = keys
@@ -603,96 +654,176 @@ def single_case(args) -> dict:
     torch.cuda.synchronize()
     rs.api.profile_enable(False)
     recs = rs.api.profile_collect()
-    agg = {}
+    agg, by_pass = {}, {}
     for r in recs:
         agg.setdefault(r["kernel"], []).append(r["ms"])
-    return {"case": args.case, "n": n, "steps": args.steps,
+        if r["kernel"] == "onesweep":
+            by_pass.setdefault(r["pass_"], []).append(r["ms"])
+    res = {}
+    if args.case.startswith("merge"):
+        ms = sum(r["ms"] for r in recs) / args.steps
+        byts = 2 * n * (4 if args.case == "merge_u32" else 8)
+        res = {"merge_GBps": round(byts / (ms * 1e-3) / 1e9, 1)}
+    return {"case": args.case, "n": n, "steps": args.steps, **res,
             "ms_per_sort": round(sum(r["ms"] for r in recs) / args.steps, 4),
-            "kernels": {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 4)} for k, v in agg.items()}}
+            "kernels": {k: {"launches": len(v), "avg_ms": round(sum(v) / len(v), 4)} for k, v in agg.items()},
+            "onesweep_ms_by_pass": {p: round(sum(v) / len(v), 4) for p, v in sorted(by_pass.items())}}
+
+
+def oracle_threads() -> int:
+    return os.cpu_count() or 1
+
+
+def config1_small(args, rs, dev, stream) -> dict:
+    """2^20 uniform uint32 keys (seed 0x5EED0001), ascending, radixsortcopynoalloc: each sort timed alone
+    with CUDA events after the L2 was flushed (the array fits in L2); checked against the oracle."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import synth as S
+    n = 1 << 20
+    a = S.uniform_bits(0x5EED0001, n, np.uint32)
+    bits = torch.from_numpy(a.view(np.int32).copy()).to(dev)
+    out, buf = torch.empty_like(bits), torch.empty_like(bits)
+    scr = torch.empty(rs.scratch_bytes(np.uint32, n), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    times = []
+    with torch.cuda.stream(stream):
+        for i in range(max(3, args.warmup) + max(10, args.steps)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rs.radixsortcopynoalloc(bits, out, buf, scr, key_dtype=np.uint32, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            if i >= max(3, args.warmup):
+                times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    from oracle import oracle as O          # the checker
+    ok = np_bytes_equal(out.cpu().numpy().view(np.uint32), O.sortcopy(a, threads=oracle_threads()))
+    del flush
+    return {"keys": n, "ms": round(ms, 4), "gkeys_s": round(n / (ms * 1e-3) / 1e9, 3),
+            "timing": "median of single sorts, L2 flushed before each (256 MiB write)",
+            "checked": "bit-exact vs oracle" if ok else "FAILED vs oracle"}
+
+
+def config3_records(args, rs, dev, stream, peak) -> dict:
+    """2^26 records of 24 bytes {u64 id, f64 key, u32 tag, pad}, key lognormal(0, 2) x random sign with
+    10% duplicated keys; the pointer array sorted by the key at byte 8, ascending
+    (radixsortcopynoalloc, member indirection); exact pointer order checked against the oracle."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import api, synth as S
+    n = 1 << 26
+    rec = S.records24_torch(S.RECORDS_SEED, n, device=dev)
+    base = rec.data_ptr()
+    ptrs = torch.arange(n, dtype=torch.int64, device=dev) * 24 + base
+    out, buf = torch.empty_like(ptrs), torch.empty_like(ptrs)
+    scr = torch.empty(rs.scratch_bytes(np.float64, n, indirection=api.MEMBER, offset1=8), dtype=torch.uint8,
+                      device=dev)
+    run = lambda: rs.radixsortcopynoalloc_member(ptrs, out, buf, scr, np.float64, 8, stream=stream)
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            run()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    assert rs.scratch_status(scr, stream) == 0
+    ms = e0.elapsed_time(e1) / args.steps
+    algo = 8 * 2 * 16 * n                     # 8 digit passes x read + write of key and pointer
+    got = (out.cpu().numpy() - base) // 24
+    rec_h = np.ascontiguousarray(rec.cpu().numpy())
+    del rec, ptrs, out, buf, scr
+    torch.cuda.empty_cache()
+    from oracle import oracle as O          # the checker
+    hb = rec_h.ctypes.data
+    hp = np.uint64(hb) + np.arange(n, dtype=np.uint64) * np.uint64(24)
+    want = (O.sortcopy_indirect(hp, np.float64, 8, "native", "ascfwdorder", threads=oracle_threads())
+            - np.uint64(hb)) // np.uint64(24)
+    ok = bool(np.array_equal(got, want.astype(np.int64)))
+    return {"keys": n, "ms": round(ms, 4), "gkeys_s": round(n / (ms * 1e-3) / 1e9, 3),
+            "algorithmic_bytes": algo, "roofline_frac": round(algo / (ms * 1e-3) / 1e9 / peak, 4),
+            "checked": "bit-exact pointer order vs oracle" if ok else "FAILED vs oracle"}
+
+
+def batched_run(args, which: str, steps: int, check: bool) -> dict:
+    """One batch of the batched configuration: one captured CUDA graph of the segmented sort, replayed
+    `steps` times, against the per-array loop of plain noalloc sorts on the same GPU; every segment
+    compared with the oracle (check) and the loop's output with the batched output."""
+    import numpy as np
+    import torch
+    from radixsortbidi8_gb300 import batched as B, synth as S
+    dev = torch.device("cuda", torch.cuda.current_device())
+    lens = S.batch_lengths(which, args.batch_scale)
+    offs = np.zeros(lens.size + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    total = int(offs[-1])
+    kdt = np.uint32 if which.startswith("A") else np.float64
+    keys = S.batch_keys_torch(which, total, device=dev)
+    off_t = torch.from_numpy(offs).to(dev)
+    sorter = B.SegmentedSorter(keys, off_t, key_dtype=kdt).capture()
+    for _ in range(max(1, args.warmup)):
+        sorter.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(sorter.stream)
+    for _ in range(steps):
+        sorter.replay()
+    e1.record(sorter.stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    assert sorter.status() == 0
+    loop_out = torch.empty_like(keys)
+    ls = torch.cuda.Stream(device=dev)
+    B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)      # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)
+    torch.cuda.synchronize()
+    loop_ms = (time.perf_counter() - t0) * 1e3
+    same = bool(torch.equal(loop_out, sorter.output))
+    res = {"arrays": int(lens.size), "keys": total, "batched_ms": round(ms, 3),
+           "batched_gkeys_s": round(total / (ms * 1e-3) / 1e9, 3), "loop_ms": round(loop_ms, 2),
+           "loop_gkeys_s": round(total / (loop_ms * 1e-3) / 1e9, 3),
+           "speedup_vs_loop": round(loop_ms / ms, 2), "identical_to_loop": same,
+           "tuning": {"small_variant": sorter.tuning.small_variant, "small_cutoff": sorter.tuning.small_cutoff}}
+    if check:
+        got = sorter.output.cpu().numpy().view(kdt)
+        a = keys.cpu().numpy().view(kdt)
+        from oracle import oracle as O          # the checker
+        want = O.sortcopy_segments(a, offs, "native", "ascfwdorder", threads=oracle_threads())
+        res["checked"] = "every segment bit-exact vs oracle" if np_bytes_equal(got, want) else "FAILED vs oracle"
+    del keys, off_t, sorter, loop_out
+    torch.cuda.empty_cache()
+    return res
 
 
 def batched_config(args) -> dict:
     """Batch A: 100,000 uint32 arrays, lengths log-uniform [16, 2^20] (seed 0x5EED0005), also truncated
-    at a cumulative 2^28 keys; batch B: 20,000 float64 arrays, log-uniform [64, 2^18] (seed 0x5EED0006).
-    Each batch: one captured CUDA graph per batch (segmented sort), replayed --steps times, against a
-    per-array loop of plain noalloc sorts on the same GPU; outputs compared byte for byte."""
-    import numpy as np
-    import torch
-    from radixsortbidi8_gb300 import batched as B, synth as S
-    dev = torch.device("cuda", 0)
-    res = {}
-
-    def one(name, key_bytes, kdt, lens, seed):
-        offs = np.zeros(lens.size + 1, dtype=np.int64)
-        np.cumsum(lens, out=offs[1:])
-        total = int(offs[-1])
-        t = {4: torch.int32, 8: torch.int64}[key_bytes]
-        keys = torch.empty(total, dtype=t, device=dev)
-        chunk = 1 << 27
-        for o in range(0, total, chunk):
-            m = min(chunk, total - o)
-            keys[o:o + m] = S.uniform_bits_torch(seed + o, m, key_bytes, device=dev) if key_bytes == 4 else \
-                S.float_specials_torch(seed + o, m, 8, device=dev)
-        off_t = torch.from_numpy(offs).to(dev)
-        sorter = B.SegmentedSorter(keys, off_t, key_dtype=kdt).capture()
-        for _ in range(max(1, args.warmup)):
-            sorter.replay()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(sorter.stream)
-        for _ in range(args.steps):
-            sorter.replay()
-        e1.record(sorter.stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        assert sorter.status() == 0
-        loop_out = torch.empty_like(keys)
-        ls = torch.cuda.Stream(device=dev)
-        B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)      # warm
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        B.sort_each(keys, loop_out, offs, key_dtype=kdt, stream=ls)
-        torch.cuda.synchronize()
-        loop_ms = (time.perf_counter() - t0) * 1e3
-        same = bool(torch.equal(loop_out, sorter.output))
-        res[name] = {"arrays": int(lens.size), "keys": total, "batched_ms": round(ms, 3),
-                     "batched_gkeys_s": round(total / (ms * 1e-3) / 1e9, 3), "loop_ms": round(loop_ms, 2),
-                     "loop_gkeys_s": round(total / (loop_ms * 1e-3) / 1e9, 3),
-                     "speedup_vs_loop": round(loop_ms / ms, 2), "identical_to_loop": same,
-                     "tuning": {"small_variant": sorter.tuning.small_variant,
-                                "small_cutoff": sorter.tuning.small_cutoff}}
-        del keys, off_t, sorter, loop_out
-        torch.cuda.empty_cache()
-
-    na = max(1, int(100000 * args.batch_scale))
-    lens_a = S.log_uniform_lengths(0x5EED0005, na, 16, 1 << 20)
-    cut = int(np.searchsorted(np.cumsum(lens_a), 1 << 28))
-    one("A_2p28", 4, np.uint32, lens_a[:max(1, cut)], 0x5EED0005)
-    one("A", 4, np.uint32, lens_a, 0x5EED0005)
-    nb = max(1, int(20000 * args.batch_scale))
-    one("B", 8, np.float64, S.log_uniform_lengths(0x5EED0006, nb, 64, 1 << 18), 0x5EED0006)
+    at a cumulative 2^28 keys; batch B: 20,000 float64 arrays, log-uniform [64, 2^18] (seed 0x5EED0006)."""
+    res = {w: batched_run(args, w, args.steps, check=not args.no_cpu) for w in ("A_2p28", "A", "B")}
     return {"config": "batched segmented sort (one captured CUDA graph per batch) vs per-array loop",
             "steps": args.steps, "results": res}
 
 
-def serving_config(args) -> dict:
-    """Poisson arrivals at --rate req/s for --duration s; length log-uniform [2^10, 2^26]; key type
+def serving_run(args, rate: float, duration: float, closed: int, checks: int) -> dict:
+    """Poisson arrivals at `rate` req/s for `duration` s; length log-uniform [2^10, 2^26]; key type
     uniform over {uint16, int32, float32, float64}; direction asc/desc (forward order); absolute filter
     with probability 0.5; 64 GB device budget.  Inputs are slices of device-resident pools (the loop
-    measures sort service, not host transfers).  Then the same requests, closed-loop: all queued at
-    once through the server vs a loop of plain allocating sorts."""
+    measures sort service, not host transfers).  Then the first `closed` requests, closed-loop: all
+    queued at once through the server vs a loop of plain allocating sorts.  `checks` served results
+    (spread over the run, the largest request included) are compared with the oracle."""
     import numpy as np
     import torch
-    from radixsortbidi8_gb300 import serving, synth as S, api
-    dev = torch.device("cuda", 0)
-    arr = S.poisson_arrivals(0x5EED0007, args.rate, args.duration)
+    from radixsortbidi8_gb300 import serving, synth as S
+    import radixsortbidi8_gb300 as rs
+    dev = torch.device("cuda", torch.cuda.current_device())
+    arr, lens, kind, desc, absf = S.serving_requests(rate, duration)
     nreq = arr.size
-    lens = S.log_uniform_lengths(0x5EED0007, nreq, 1 << 10, 1 << 26)
-    u = S.splitmix64(0x5EED0007, nreq, stream=41)
     kinds = [(np.uint16, torch.int16), (np.int32, torch.int32), (np.float32, torch.int32), (np.float64, torch.int64)]
-    kind = (u % np.uint64(4)).astype(int)
-    desc = (S.splitmix64(0x5EED0007, nreq, stream=42) & np.uint64(1)).astype(int)
-    absf = (S.splitmix64(0x5EED0007, nreq, stream=43) & np.uint64(1)).astype(int)
     pool_n = 1 << 27
     pools = []
     for kd, td in kinds:
@@ -704,9 +835,12 @@ def serving_config(args) -> dict:
     rings = [torch.empty(ring_n, dtype=td, device=dev) for _, td in kinds]
     ring_pos = [0, 0, 0, 0]
     ring_owner = [[], [], [], []]           # (start, end, request id) still possibly in flight
-    starts = (S.splitmix64(0x5EED0007, nreq, stream=44) % np.uint64(pool_n - (1 << 26))).astype(np.int64)
+    starts = (S.splitmix64(S.SERVING_SEED, nreq, stream=44) % np.uint64(pool_n - (1 << 26))).astype(np.int64)
     srv = serving.Server(budget_bytes=64 << 30, max_inflight=4)
     ids, metas = [], []
+
+    def dm(i):
+        return ("dscfwdorder" if desc[i] else "ascfwdorder"), ("nativeabs" if absf[i] else "native")
 
     def out_region(k, n):
         p = ring_pos[k] if ring_pos[k] + n <= ring_n else 0
@@ -727,13 +861,9 @@ def serving_config(args) -> dict:
             time.sleep(delay)
         k = kind[i]
         n = int(lens[i])
-        kd = kinds[k][0]
         p = out_region(k, n)
-        inp = pools[k][starts[i]:starts[i] + n]
-        out = rings[k][p:p + n]
-        d = "dscfwdorder" if desc[i] else "ascfwdorder"
-        m = "nativeabs" if absf[i] else "native"
-        rid = srv.submit(inp, out, d, m, key_dtype=kd)
+        d, m = dm(i)
+        rid = srv.submit(pools[k][starts[i]:starts[i] + n], rings[k][p:p + n], d, m, key_dtype=kinds[k][0])
         ring_owner[k].append((p, p + n, rid))
         ids.append(rid)
         metas.append((k, n, d, m, int(starts[i]), p))
@@ -744,56 +874,87 @@ def serving_config(args) -> dict:
     t_last = max(i.done_s for i in infos)
     keys = int(sum(i.count for i in infos))
     lat = serving.latency_summary(infos)
-    # spot check: a few results against a standalone sort of the same request
-    ok = True
-    for j in list(range(0, nreq, max(1, nreq // 16)))[:16]:
+    # checks: results whose output region no later request of the same key type overwrote, against
+    # the oracle
+    from oracle import oracle as O          # the checker
+    kk = np.array([m[0] for m in metas])
+    pp = np.array([m[5] for m in metas], dtype=np.int64)
+    nn = np.array([m[1] for m in metas], dtype=np.int64)
+    cand = []
+    for j in range(nreq):
+        later = np.nonzero(kk[j + 1:] == kk[j])[0] + j + 1
+        if not np.any((pp[later] < pp[j] + nn[j]) & (pp[j] < pp[later] + nn[later])):
+            cand.append(j)
+    pick = sorted(set(cand[::max(1, len(cand) // max(1, checks - 1))][:max(0, checks - 1)] +
+                      ([max(cand, key=lambda j: metas[j][1])] if cand else []))) if checks > 0 else []
+    items, gots = [], []
+    for j in pick:
         k, n, d, m, s0, p = metas[j]
-        if p + n > ring_n or any(a < p + n and p < b for (a, b, r) in ring_owner[k] if r > ids[j]):
-            continue
-        alone = torch.empty(n, dtype=kinds[k][1], device=dev)
-        import radixsortbidi8_gb300 as rs
-        rs.radixsortcopy(pools[k][s0:s0 + n], alone, d, m, key_dtype=kinds[k][0])
-        ok &= bool(torch.equal(alone, rings[k][p:p + n]))
+        kd = kinds[k][0]
+        items.append((pools[k][s0:s0 + n].cpu().numpy().view(kd), m, d))
+        gots.append(rings[k][p:p + n].cpu().numpy().view(kd))
+    wants = O.sortcopy_batch(items, threads=oracle_threads()) if items else []
+    bad = sum(not np_bytes_equal(g, w) for g, w in zip(gots, wants))
     srv.close()
+    del rings
+    torch.cuda.empty_cache()
     # closed loop: a prefix of the same requests, queued at once vs a plain allocating-sort loop
-    m_req = min(nreq, 2000)
+    m_req = min(nreq, closed)
     outs = [torch.empty(int(lens[i]), dtype=kinds[kind[i]][1], device=dev) for i in range(m_req)]
     srv2 = serving.Server(budget_bytes=64 << 30, max_inflight=4)
     for i in range(min(m_req, 64)):          # warm-up of kernels and module loading
-        srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
-                    "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
-                    key_dtype=kinds[kind[i]][0])
+        d, m = dm(i)
+        srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i], d, m, key_dtype=kinds[kind[i]][0])
     srv2.drain()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ids2 = [srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
-                        "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
-                        key_dtype=kinds[kind[i]][0]) for i in range(m_req)]
+    ids2 = []
+    for i in range(m_req):
+        d, m = dm(i)
+        ids2.append(srv2.submit(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i], d, m,
+                                key_dtype=kinds[kind[i]][0]))
     srv2.drain()
     served_s = time.perf_counter() - t0
     st2 = srv2.stats()
     srv2.close()
-    import radixsortbidi8_gb300 as rs
+    # the closed loop's results, the largest requests included, against the oracle
+    cpick = sorted(set(list(range(0, m_req, max(1, m_req // max(1, checks - 1))))[:max(0, checks - 1)] +
+                       [int(np.argmax(lens[:m_req]))])) if checks > 0 and m_req > 0 else []
+    citems, cgots = [], []
+    for i in cpick:
+        d, m = dm(i)
+        kd = kinds[kind[i]][0]
+        citems.append((pools[kind[i]][starts[i]:starts[i] + int(lens[i])].cpu().numpy().view(kd), m, d))
+        cgots.append(outs[i].cpu().numpy().view(kd))
+    cwants = O.sortcopy_batch(citems, threads=oracle_threads()) if citems else []
+    cbad = sum(not np_bytes_equal(g, w) for g, w in zip(cgots, cwants))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(m_req):
-        rs.radixsortcopy(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i],
-                         "dscfwdorder" if desc[i] else "ascfwdorder", "nativeabs" if absf[i] else "native",
+        d, m = dm(i)
+        rs.radixsortcopy(pools[kind[i]][starts[i]:starts[i] + int(lens[i])], outs[i], d, m,
                          key_dtype=kinds[kind[i]][0])
     torch.cuda.synchronize()
     loop_s = time.perf_counter() - t0
     keys2 = int(lens[:m_req].sum())
-    del ids2, api
-    return {"config": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s, lengths log-uniform "
+    del outs
+    torch.cuda.empty_cache()
+    return {"config": f"serving: Poisson {rate:g} req/s for {duration:g} s, lengths log-uniform "
                       f"[2^10, 2^26], {{u16, i32, f32, f64}}, asc/desc, abs p=0.5, 64 GB budget",
-            "requests": nreq, "offered_gkeys_s": round(float(lens.sum()) / args.duration / 1e9, 3),
+            "requests": nreq, "offered_gkeys_s": round(float(lens.sum()) / duration / 1e9, 3),
             "served_gkeys_s": round(keys / (t_last - t_first) / 1e9, 3), "latency": lat,
-            "batches": st["batches"], "max_coalesced": st["max_coalesced"],
-            "max_inflight_batches": st["max_inflight_batches"], "spot_checks_identical": ok,
+            "batches": st["batches"], "launches_per_request": round(st["batches"] / max(1, nreq), 3),
+            "max_coalesced": st["max_coalesced"], "max_inflight_batches": st["max_inflight_batches"],
+            "checked": f"{len(pick) - bad} of {len(pick)} served results bit-exact vs oracle",
             "closed_loop": {"requests": m_req, "keys": keys2,
                             "served_gkeys_s": round(keys2 / served_s / 1e9, 3),
                             "plain_loop_gkeys_s": round(keys2 / loop_s / 1e9, 3),
-                            "speedup": round(loop_s / served_s, 2), "batches": st2["batches"]}}
+                            "speedup": round(loop_s / served_s, 2), "batches": st2["batches"],
+                            "checked": f"{len(cpick) - cbad} of {len(cpick)} results bit-exact vs oracle"}}
+
+
+def serving_config(args) -> dict:
+    return serving_run(args, args.rate, args.duration, 2000, 64)
 
 
 def main():

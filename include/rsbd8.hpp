@@ -24,8 +24,8 @@
 //   longdoubletest128; binary128 where long double is that)   Radixsortbidi8.hpp:1061-2404, :2849
 // Getters are evaluated on the host for every element (C++ member functions cannot be
 // called from the device), so their objects must be host-accessible; the keys then travel
-// to the device and the pointers are sorted there.  Getters are offered in the allocating
-// forms only: the noalloc forms could not hold the host-evaluated keys.
+// to the device and the pointers are sorted there.  The noalloc getter forms keep those keys
+// in the tail of the caller's scratch (rsbd8::gpuscratchbytesgetter).
 #pragma once
 
 #include <cuda_runtime_api.h>
@@ -34,6 +34,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -419,29 +420,131 @@ radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplace
 }
 
 // ---- getter member function (evaluated on the host), with optional extra arguments ----------------
+// The key of element i is what input[i]->*getter returns (splitgetfunction, Radixsortbidi8.hpp:
+// 2646-2706; indirectinput1 :2768-2784): the returned value itself, or -- when the getter returns a
+// pointer or an lvalue reference -- the key at byte indirection2 behind it, the index2-th key there
+// with isindexed2 (indirectinput2 :2806-2812).  With isindexed2 the first extra argument is index2
+// and the others go to the getter.  The facade calls the getter on the host for every element (the
+// objects, and what the getter returns a pointer to, must be host-accessible), copies the keys to
+// the device and sorts the pointers by them there.
+
+namespace gpu_detail {
+
+template <auto getter, typename V, typename... A>
+using getterresult = decltype((std::declval<V *>()->*getter)(std::declval<A>()...));
+
+// the getter's result type with the extra arguments it is called with (index2 split off)
+template <auto getter, bool isindexed2, typename V, typename... A>
+struct gettercall;
+template <auto getter, typename V, typename... A>
+struct gettercall<getter, false, V, A...> {
+    using result = getterresult<getter, V, A...>;
+};
+template <auto getter, typename V, typename I, typename... A>
+struct gettercall<getter, true, V, I, A...> {
+    static_assert(std::is_integral_v<std::remove_cv_t<std::remove_reference_t<I>>>, "isindexed2: the first extra argument is the index");
+    using result = getterresult<getter, V, A...>;
+};
+
+template <typename R>
+constexpr bool getterpoints{std::is_lvalue_reference_v<R> || std::is_pointer_v<std::remove_reference_t<R>>};
+
+template <typename R>
+using getterkey = std::remove_cv_t<std::conditional_t<std::is_lvalue_reference_v<R>, std::remove_reference_t<R>,
+                                                      std::remove_pointer_t<std::remove_reference_t<R>>>>;
+
+// the key of one element from the getter's result
+template <typename K, std::ptrdiff_t indirection2, typename R>
+inline K keyfromresult(R &&r, std::ptrdiff_t index2) {
+    K k;
+    if constexpr (std::is_lvalue_reference_v<R>) {
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(std::addressof(r));
+        std::memcpy(&k, b + indirection2 + index2 * std::ptrdiff_t(sizeof(K)), sizeof(K));
+    } else if constexpr (std::is_pointer_v<std::remove_reference_t<R>>) {
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(r);
+        std::memcpy(&k, b + indirection2 + index2 * std::ptrdiff_t(sizeof(K)), sizeof(K));
+    } else {
+        std::memcpy(&k, &r, sizeof(K));
+    }
+    return k;
+}
+
+template <auto getter, std::ptrdiff_t indirection2, typename K, typename V, typename... A>
+inline void getkeys(std::size_t count, V *const *p, K *keys, std::false_type, A &&...a) {
+    for (std::size_t i = 0; i < count; ++i) keys[i] = keyfromresult<K, indirection2>((p[i]->*getter)(a...), 0);
+}
+template <auto getter, std::ptrdiff_t indirection2, typename K, typename V, typename I, typename... A>
+inline void getkeys(std::size_t count, V *const *p, K *keys, std::true_type, I &&index2, A &&...a) {
+    for (std::size_t i = 0; i < count; ++i)
+        keys[i] = keyfromresult<K, indirection2>((p[i]->*getter)(a...), std::ptrdiff_t(index2));
+}
+
+template <auto getter, std::ptrdiff_t indirection2, bool isindexed2, typename V, typename... A>
+struct getterinfo {
+    using R = typename gettercall<getter, isindexed2, V, A...>::result;
+    using K = getterkey<R>;
+    static_assert(getterpoints<R> || (!isindexed2 && indirection2 == 0),
+                  "a getter that returns the key itself takes neither indirection2 nor isindexed2");
+    static_assert(!std::is_pointer_v<K>, "third level indirection is not supported");
+    static_assert(iskeytype<K>, "unsupported key type");
+};
+
+// the pointers of input (device or host memory) on the host, ordered after the stream's work
+template <typename V>
+inline bool hostpointers(std::size_t count, V *const *input, std::vector<V *> &ptrs) {
+    ptrs.resize(count);
+    return cudaMemcpyAsync(ptrs.data(), input, count * sizeof(V *), cudaMemcpyDefault,
+                           reinterpret_cast<cudaStream_t>(stream_slot())) == cudaSuccess &&
+           cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream_slot())) == cudaSuccess;
+}
+
+// every element's key evaluated on the host, then copied to `dkeys` (device) on the stream
+template <auto getter, std::ptrdiff_t indirection2, bool isindexed2, typename V, typename... A>
+inline bool hostkeys(std::size_t count, V *const *input, void *dkeys, A &&...a) {
+    using K = typename getterinfo<getter, indirection2, isindexed2, V, A...>::K;
+    std::vector<V *> ptrs;
+    if (!hostpointers(count, input, ptrs)) return false;
+    std::vector<K> keys(count);
+    getkeys<getter, indirection2, K>(count, ptrs.data(), keys.data(), std::bool_constant<isindexed2>{},
+                                     std::forward<A>(a)...);
+    // a copy from pageable memory is staged before the call returns: `keys` may go
+    return cudaMemcpyAsync(dkeys, keys.data(), count * sizeof(K), cudaMemcpyHostToDevice,
+                           reinterpret_cast<cudaStream_t>(stream_slot())) == cudaSuccess;
+}
+
+inline std::size_t keyedscratch(const rsbd8g_desc &d, std::size_t count) {
+    std::size_t b = 0;
+    return rsbd8g_scratch_bytes(&d, count, &b) == RSBD8G_OK ? (b + 255u) & ~std::size_t(255u) : 0;
+}
+
+}  // namespace gpu_detail
+
+// Scratch bytes (device) of the noalloc forms with a getter whose keys have type K: the sort's own
+// scratch, then room for the keys the host evaluates.
+template <sortingdirection direction = sortingdirection::ascfwdorder, sortingmode mode = sortingmode::native,
+          typename K>
+inline std::size_t gpuscratchbytesgetter(std::size_t count) noexcept {
+    return gpu_detail::keyedscratch(gpu_detail::makedesc<direction, mode, K>(RSBD8G_KEYED), count) + count * sizeof(K);
+}
 
 template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
           sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
           typename V, typename... vararguments>
 [[nodiscard]] inline std::enable_if_t<std::is_member_function_pointer_v<decltype(indirection1)>, bool>
 radixsortcopy(std::size_t count, V *const *input, V **output, int mmapflags = 0, vararguments &&...varparameters) {
-    static_assert(indirection2 == 0 && !isindexed2, "getter results are the keys themselves on the GPU path");
+    using info = gpu_detail::getterinfo<indirection1, indirection2, isindexed2, V, vararguments...>;
+    using K = typename info::K;
     static_cast<void>(mmapflags);
-    using T = std::remove_cv_t<std::remove_reference_t<decltype((std::declval<V *>()->*indirection1)(varparameters...))>>;
-    static_assert(gpu_detail::iskeytype<T>, "unsupported getter result type");
     if (count < 2) {
         if (count == 1) return cudaMemcpy(output, input, sizeof(V *), cudaMemcpyDefault) == cudaSuccess;
         return true;
     }
-    std::vector<V *> ptrs(count);
-    if (cudaMemcpy(ptrs.data(), input, count * sizeof(V *), cudaMemcpyDefault) != cudaSuccess) return false;
-    std::vector<T> keys(count);
-    for (std::size_t i = 0; i < count; ++i) keys[i] = (ptrs[i]->*indirection1)(varparameters...);
     void *dkeys = nullptr;
-    if (cudaMalloc(&dkeys, count * sizeof(T)) != cudaSuccess) return false;
-    bool good = cudaMemcpy(dkeys, keys.data(), count * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (cudaMalloc(&dkeys, count * sizeof(K)) != cudaSuccess) return false;
+    bool good = gpu_detail::hostkeys<indirection1, indirection2, isindexed2>(
+        count, input, dkeys, std::forward<vararguments>(varparameters)...);
     if (good) {
-        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, T>(RSBD8G_KEYED);
+        rsbd8g_desc d = gpu_detail::makedesc<direction, mode, K>(RSBD8G_KEYED);
         good = gpu_detail::ok(rsbd8g_radixsortcopy_keyed(&d, count, dkeys, input, output, gpu_detail::stream_slot()));
     }
     cudaFree(dkeys);
@@ -461,6 +564,55 @@ radixsort(std::size_t count, V **input, int mmapflags = 0, vararguments &&...var
     if (good) good = cudaMemcpy(input, tmp, count * sizeof(V *), cudaMemcpyDefault) == cudaSuccess;
     cudaFree(tmp);
     return good;
+}
+
+// The noalloc forms with a getter: pzeroedindices is device scratch of gpuscratchbytesgetter<...,
+// K>(count) bytes; the keys evaluated on the host are stored in its tail.  These forms wait for the
+// stream before they read the input pointers on the host; the sort itself is stream-ordered.
+template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... vararguments>
+inline std::enable_if_t<std::is_member_function_pointer_v<decltype(indirection1)>, void>
+radixsortcopynoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                     V *const *input, V **output, V **buffer, vararguments &&...varparameters) {
+    using K = typename gpu_detail::getterinfo<indirection1, indirection2, isindexed2, V, vararguments...>::K;
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    if (count < 2) {
+        if (count == 1) cudaMemcpy(output, input, sizeof(V *), cudaMemcpyDefault);
+        return;
+    }
+    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, K>(RSBD8G_KEYED);
+    const std::size_t own = gpu_detail::keyedscratch(d, count);
+    void *dkeys = static_cast<unsigned char *>(pzeroedindices) + own;
+    if (!gpu_detail::hostkeys<indirection1, indirection2, isindexed2>(count, input, dkeys,
+                                                                        std::forward<vararguments>(varparameters)...))
+        return;
+    rsbd8g_radixsortcopynoalloc_keyed(&d, count, dkeys, pzeroedindices, own, input, output, buffer,
+                                      gpu_detail::stream_slot());
+}
+
+template <auto indirection1, sortingdirection direction = sortingdirection::ascfwdorder,
+          sortingmode mode = sortingmode::native, std::ptrdiff_t indirection2 = 0, bool isindexed2 = false,
+          typename V, typename... vararguments>
+inline std::enable_if_t<std::is_member_function_pointer_v<decltype(indirection1)>, void>
+radixsortnoalloc(std::size_t count, unsigned allowedthreads, void *pfuturesplaceholder, void *pzeroedindices,
+                 V **input, V **buffer, bool movetobuffer = false, vararguments &&...varparameters) {
+    using K = typename gpu_detail::getterinfo<indirection1, indirection2, isindexed2, V, vararguments...>::K;
+    static_cast<void>(allowedthreads);
+    static_cast<void>(pfuturesplaceholder);
+    if (count < 2) {
+        if (count == 1 && movetobuffer) cudaMemcpy(buffer, input, sizeof(V *), cudaMemcpyDefault);
+        return;
+    }
+    rsbd8g_desc d = gpu_detail::makedesc<direction, mode, K>(RSBD8G_KEYED);
+    const std::size_t own = gpu_detail::keyedscratch(d, count);
+    void *dkeys = static_cast<unsigned char *>(pzeroedindices) + own;
+    if (!gpu_detail::hostkeys<indirection1, indirection2, isindexed2>(count, input, dkeys,
+                                                                        std::forward<vararguments>(varparameters)...))
+        return;
+    rsbd8g_radixsortnoalloc_keyed(&d, count, dkeys, pzeroedindices, own, input, buffer, movetobuffer ? 1 : 0,
+                                  gpu_detail::stream_slot());
 }
 
 // ---- type + offset: <T, indirection1, direction, mode, indirection2, isindexed2> ------------------

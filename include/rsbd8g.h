@@ -100,7 +100,7 @@ enum {
 #define RSBD8G_FLAG_DEVICE_ARRAYS 4u
 
 typedef struct rsbd8g_desc {
-    uint32_t key_bytes;     /* 1, 2, 4, 8 or 16 (16: not in the segmented and serving entry points) */
+    uint32_t key_bytes;     /* 1, 2, 4, 8 or 16 (x87 keys: not in the segmented and serving entry points) */
     uint32_t key_kind;      /* RSBD8G_KIND_* */
     uint32_t mode;          /* rsbd8::sortingmode value */
     uint32_t direction;     /* rsbd8::sortingdirection value */
@@ -131,6 +131,19 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy(const rsbd8g_desc *desc, size_t co
  * function pointer; the getter call itself is splitget, Radixsortbidi8.hpp:2405-2719). */
 RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
                                                     const void *input, void *output, rsbd8g_stream stream);
+
+/* The noalloc forms of rsbd8g_radixsortcopy_keyed (desc->indirection == RSBD8G_KEYED): `keys`
+ * (count raw keys, device-accessible) are read, not written; scratch as sized by
+ * rsbd8g_scratch_bytes for this descriptor; buffer of count 8-byte values.  Stream-ordered.
+ * The C++ facade's noalloc getter forms use them.
+ * Replaces: rsbd8::radixsortcopynoalloc / radixsortnoalloc with a getter member function
+ * (Radixsortbidi8.hpp:60983, :61018). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopynoalloc_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                           void *scratch, size_t scratch_bytes, const void *input,
+                                                           void *output, void *buffer, rsbd8g_stream stream);
+RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                       void *scratch, size_t scratch_bytes, void *input, void *buffer,
+                                                       int movetobuffer, rsbd8g_stream stream);
 
 /* Sort `count` elements of `input` in place.  Allocates, blocks until done.
  * Replaces: rsbd8::radixsort (Radixsortbidi8.hpp:60398). */
@@ -185,6 +198,32 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_static(const rsbd8g_desc *desc, si
  * nothing.  No counterpart in the reference (its functions report no device state). */
 RSBD8G_API rsbd8g_status rsbd8g_static_status(rsbd8g_stream stream);
 
+/* ---- merges of sorted runs, and arrays larger than the device ------------------------------
+ * rsbd8g_merge_runs: stable merge of `nruns` runs that lie back to back in `input` (device
+ * memory), each sorted by `desc` (direct keys), into `output`; run r holds run_counts[r] elements
+ * (run_counts is a host array).  On equal filtered keys the earlier run goes first, or the later
+ * run when the direction has reverse order and the mode honours it (as in the sort).  Two runs
+ * merge straight into `output`; more runs take `buffer` (as many elements as the runs together;
+ * it may be null for two runs).  Stream-ordered; allocates nothing.
+ * Replaces: the merges of the halves and thirds that the reference's threads sort
+ * (mergehalvesmtc / mergehalvesmain, Radixsortbidi8.hpp:54437, :54815; mergethirdsmtc /
+ * mergethirdsmain, :55369, :56014): with run_counts {count / 2, count - count / 2} or
+ * {count / 3, (count + 1) / 3, the rest} it merges the same parts into the same order. */
+RSBD8G_API rsbd8g_status rsbd8g_merge_runs(const rsbd8g_desc *desc, size_t nruns, const size_t *run_counts,
+                                           const void *input, void *output, void *buffer, rsbd8g_stream stream);
+
+/* Sort `count` keys held in HOST memory (input and output host arrays; pinned memory copies
+ * fastest), with the semantics of rsbd8g_radixsortcopy, using at most `device_bytes` of device
+ * memory (0: nine tenths of the free memory).  An array whose in-place sort (array, ping-pong
+ * buffer, scratch) fits that budget is sorted in one piece; a larger one is sorted in chunks that
+ * fit, kept as sorted runs in a host buffer, and merged block by block on the device.  Allocates
+ * (device memory within the budget, a host buffer of `count` keys), blocks until done.  Direct keys.
+ * Replaces: rsbd8::radixsortcopy (Radixsortbidi8.hpp:60476) for arrays that do not fit the GPU;
+ * the split into parts sorted apart and merged is the reference's own multithreaded scheme
+ * (Radixsortbidi8.hpp:55100-55160). */
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_chunked(const rsbd8g_desc *desc, size_t count, const void *input,
+                                                      void *output, size_t device_bytes, rsbd8g_stream stream);
+
 /* ---- batched (segmented) sort -------------------------------------------------------------
  * Many independent arrays of uneven sizes in one stream-ordered call: segment s is elements
  * [offsets[s], offsets[s+1]) of `input` (offsets: a device array of nsegs + 1 non-decreasing
@@ -217,6 +256,17 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs(const rsbd8g_desc *desc,
                                                         const uint64_t *output_ptrs, const uint64_t *buffer_ptrs,
                                                         void *scratch, size_t scratch_bytes,
                                                         const rsbd8g_segtuning *tuning, rsbd8g_stream stream);
+
+/* The pointer-table form with a direction per segment: `directions` is a device array of nsegs
+ * bytes, each the sortingdirection value (0..3) of its segment; desc->direction is not used.  The
+ * other fields of desc (key type, mode, flags) hold for every segment.  The serving loop coalesces
+ * requests that differ only in direction through this form.  No counterpart in the reference. */
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs_dirs(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                             const uint64_t *offsets, const uint64_t *input_ptrs,
+                                                             const uint64_t *output_ptrs, const uint64_t *buffer_ptrs,
+                                                             const uint8_t *directions, void *scratch,
+                                                             size_t scratch_bytes, const rsbd8g_segtuning *tuning,
+                                                             rsbd8g_stream stream);
 
 /* ---- serving loop -------------------------------------------------------------------------
  * Continuous batching of sort requests on the current device.  rsbd8g_server_create allocates
@@ -266,7 +316,7 @@ RSBD8G_API const char *rsbd8g_status_string(rsbd8g_status status);
 
 enum {
     RSBD8G_KERNEL_MEMSET = 0, RSBD8G_KERNEL_HISTOGRAM = 1, RSBD8G_KERNEL_PLAN = 2,
-    RSBD8G_KERNEL_ONESWEEP = 3, RSBD8G_KERNEL_COPY = 4, RSBD8G_KERNEL_SEGMENTED = 5
+    RSBD8G_KERNEL_ONESWEEP = 3, RSBD8G_KERNEL_COPY = 4, RSBD8G_KERNEL_SEGMENTED = 5, RSBD8G_KERNEL_MERGE = 6
 };
 
 typedef struct rsbd8g_launch_record {

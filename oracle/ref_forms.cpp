@@ -14,6 +14,11 @@
 struct Rec {            // 24 bytes: id, then four 32-bit keys a b c d at bytes 8, 12, 16, 20
     std::uint64_t id;
     std::uint32_t a, b, c, d;
+    // getters: by value, by reference, by pointer, and by pointer chosen by an argument
+    std::uint32_t geta() const noexcept { return a; }
+    std::uint32_t const &refa() const noexcept { return a; }
+    std::uint32_t const *pointa() const noexcept { return &a; }
+    std::uint32_t const *pick(int k) const noexcept { return k ? &c : &a; }
 };
 
 int main() {
@@ -58,6 +63,13 @@ int main() {
     ok &= rsbd8::radixsortcopy<A, N, 4>(n, kin, kout); showk("second level, indirection2 4");
     ok &= rsbd8::radixsortcopy<A, N, 0, true>(n, kin, kout, F, 2); showk("second level, isindexed2, index 2");
     ok &= rsbd8::radixsortcopy<A, N, 4, true>(n, kin, kout, F, 1); showk("second level, indirection2 4, isindexed2, index 1");
+    ok &= rsbd8::radixsortcopy<&Rec::geta>(n, in, out); show("getter a");
+    ok &= rsbd8::radixsortcopy<&Rec::geta, D>(n, in, out); show("getter a desc");
+    ok &= rsbd8::radixsortcopy<&Rec::refa, A, N, 4>(n, in, out); show("getter reference a, indirection2 4");
+    ok &= rsbd8::radixsortcopy<&Rec::pointa, A, N, 0, true>(n, in, out, F, 2); show("getter pointer a, isindexed2, index 2");
+    ok &= rsbd8::radixsortcopy<&Rec::pointa, D, N, 4, true>(n, in, out, F, 2); show("getter pointer a desc, indirection2 4, isindexed2, index 2");
+    ok &= rsbd8::radixsortcopy<&Rec::pick, A, N, 0, true>(n, in, out, F, 1, 1); show("getter pick(1), isindexed2, index 1");
+    ok &= rsbd8::radixsortcopy<&Rec::pick, A, N, 4>(n, in, out, F, 0); show("getter pick(0), indirection2 4");
     std::printf("all calls returned true: %d\n", ok ? 1 : 0);
     return ok ? 0 : 1;
 }

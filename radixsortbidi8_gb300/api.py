@@ -65,7 +65,7 @@ EXPORTS = ["rsbd8g_scratch_bytes", "rsbd8g_radixsortcopy", "rsbd8g_radixsort",
            "rsbd8g_radixsortcopynoalloc", "rsbd8g_radixsortnoalloc", "rsbd8g_scratch_status",
            "rsbd8g_status_string", "rsbd8g_version", "rsbd8g_profile_enable", "rsbd8g_profile_collect"]
 
-KERNEL_NAMES = {0: "memset", 1: "histogram", 2: "plan", 3: "onesweep", 4: "copy", 5: "segmented"}
+KERNEL_NAMES = {0: "memset", 1: "histogram", 2: "plan", 3: "onesweep", 4: "copy", 5: "segmented", 6: "merge"}
 
 
 class LaunchRecord(ctypes.Structure):
@@ -100,6 +100,8 @@ def lib():
         "rsbd8g_radixsortcopy_static": ([P, S, VP, VP, VP], I32),
         "rsbd8g_static_status": ([VP], I32),
         "rsbd8g_binary_version": ([ctypes.POINTER(I32)], I32),
+        "rsbd8g_merge_runs": ([P, S, ctypes.POINTER(ctypes.c_size_t), VP, VP, VP, VP], I32),
+        "rsbd8g_radixsortcopy_chunked": ([P, S, VP, VP, S, VP], I32),
     }
     for name, (args, res) in sigs.items():
         f = getattr(L, name)
@@ -261,6 +263,55 @@ def radixsortnoalloc(input, buffer, scratch, movetobuffer: bool = False, directi
 def scratch_status(scratch, stream=None) -> int:
     """Wait for the stream and read (and clear) the device status word of a scratch area."""
     return int(lib().rsbd8g_scratch_status(_ptr(scratch), _stream(stream)))
+
+
+def merge_runs(input, output, run_counts, buffer=None, direction="ascfwdorder", mode="native", key_dtype=None,
+               stream=None) -> None:
+    """Stable merge of sorted runs lying back to back in `input` (lengths run_counts) into `output`
+    (the reference's mergehalves* / mergethirds* for its halves / thirds split); `buffer` (as long
+    as the runs together) when there are more than two runs.  Stream-ordered."""
+    d = make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode)
+    counts = (ctypes.c_size_t * max(1, len(run_counts)))(*[int(c) for c in run_counts])
+    _check(lib().rsbd8g_merge_runs(ctypes.byref(d), len(run_counts), counts, _ptr(input), _ptr(output), _ptr(buffer),
+                                   _stream(stream)), "rsbd8g_merge_runs")
+
+
+def halves(count: int) -> list[int]:
+    """The reference's split of an array into two parts (mergehalves*)."""
+    return [count // 2, count - count // 2]
+
+
+def thirds(count: int) -> list[int]:
+    """The reference's split of an array into three parts (mergethirds*)."""
+    return [count // 3, (count + 1) // 3, count - count // 3 - (count + 1) // 3]
+
+
+def radixsortcopy_chunked(input, output, direction="ascfwdorder", mode="native", key_dtype=None,
+                          device_bytes: int = 0, stream=None) -> bool:
+    """rsbd8::radixsortcopy for keys in HOST memory (numpy arrays or CPU tensors) that need not fit
+    the device: sorted in chunks within device_bytes (0: most of the free memory) and merged.
+    Blocks until done; False when the device allocation failed."""
+    def hptr(x):
+        if isinstance(x, np.ndarray):
+            if not x.flags["C_CONTIGUOUS"]:
+                raise ValueError("arrays must be contiguous")
+            return x.ctypes.data
+        if hasattr(x, "data_ptr"):
+            if x.is_cuda or not x.is_contiguous():
+                raise ValueError("arrays must be contiguous host tensors")
+            return x.data_ptr()
+        raise TypeError(f"expected a host array, got {type(x)}")
+    kd = key_dtype if key_dtype is not None else input.dtype
+    d = make_desc(kd, direction, mode)
+    n = int(input.size if isinstance(input, np.ndarray) else input.numel())
+    if d.key_bytes == 16:
+        n = n * (input.itemsize if isinstance(input, np.ndarray) else input.element_size()) // 16
+    st = lib().rsbd8g_radixsortcopy_chunked(ctypes.byref(d), n, hptr(input), hptr(output), int(device_bytes),
+                                            _stream(stream))
+    if st == ERR_NO_MEMORY:
+        return False
+    _check(st, "radixsortcopy_chunked")
+    return True
 
 
 def binary_version() -> int:

@@ -43,6 +43,9 @@ def _lib():
         L.rsbd8g_segmented_sortcopy.restype = ctypes.c_int
         L.rsbd8g_segmented_sortcopy_ptrs.argtypes = [P, S, S, VP, VP, VP, VP, VP, S, ctypes.POINTER(SegTuning), VP]
         L.rsbd8g_segmented_sortcopy_ptrs.restype = ctypes.c_int
+        L.rsbd8g_segmented_sortcopy_ptrs_dirs.argtypes = [P, S, S, VP, VP, VP, VP, VP, VP, S, ctypes.POINTER(SegTuning),
+                                                          VP]
+        L.rsbd8g_segmented_sortcopy_ptrs_dirs.restype = ctypes.c_int
         L._seg_sigs = True
     return L
 
@@ -68,15 +71,19 @@ def segmented_scratch_bytes(key_dtype, total: int, nsegs: int, direction="ascfwd
 
 
 def segmented_sortcopy_ptrs(inputs, outputs, buffers, scratch, direction="ascfwdorder", mode="native",
-                            key_dtype=None, tuning: SegTuning | None = None, stream=None, flags: int = 0):
+                            key_dtype=None, tuning: SegTuning | None = None, stream=None, flags: int = 0,
+                            directions=None):
     """Sort every device tensor of `inputs` into the tensor of `outputs` at the same place, using the
     tensor of `buffers` there (rsbd8g_segmented_sortcopy_ptrs: one segment per array, in one call).
     Stream-ordered; read device errors with api.scratch_status.  flags may carry
     api.FLAG_DEVICE_ARRAYS when every array is device memory (tiles are then prefetched into L2).
+    With `directions` (one sortingdirection name or value per array) every array is sorted in its
+    own direction (rsbd8g_segmented_sortcopy_ptrs_dirs) and `direction` is not used.
     Returns the device pointer tables and offsets: keep them until the call's work is done."""
     import torch
     dev = inputs[0].device
-    lens = [int(x.numel()) for x in inputs]
+    kb = api.key_kind(key_dtype if key_dtype is not None else inputs[0].dtype)[1]
+    lens = [int(x.numel() * x.element_size() // kb) for x in inputs]
     offs = torch.zeros(len(lens) + 1, dtype=torch.int64)
     offs[1:] = torch.cumsum(torch.tensor(lens, dtype=torch.int64), 0)
     tabs = [torch.tensor([api._ptr(x) if x.numel() else 0 for x in arrs], dtype=torch.int64).to(dev)
@@ -84,6 +91,14 @@ def segmented_sortcopy_ptrs(inputs, outputs, buffers, scratch, direction="ascfwd
     offs = offs.to(dev)
     d = api.make_desc(key_dtype if key_dtype is not None else inputs[0].dtype, direction, mode, flags=flags)
     t = tuning if tuning is not None else tuning_for(d.key_bytes)
+    if directions is not None:
+        dirs = torch.tensor([api._direction(x) for x in directions], dtype=torch.uint8).to(dev)
+        tabs.append(dirs)
+        api._check(_lib().rsbd8g_segmented_sortcopy_ptrs_dirs(
+            ctypes.byref(d), int(offs[-1]), len(lens), api._ptr(offs), api._ptr(tabs[0]), api._ptr(tabs[1]),
+            api._ptr(tabs[2]), dirs.data_ptr(), api._ptr(scratch), scratch.numel() * scratch.element_size(),
+            ctypes.byref(t), api._stream(stream)), "rsbd8g_segmented_sortcopy_ptrs_dirs")
+        return tabs, offs
     api._check(_lib().rsbd8g_segmented_sortcopy_ptrs(
         ctypes.byref(d), int(offs[-1]), len(lens), api._ptr(offs), api._ptr(tabs[0]), api._ptr(tabs[1]),
         api._ptr(tabs[2]), api._ptr(scratch), scratch.numel() * scratch.element_size(), ctypes.byref(t),
@@ -99,7 +114,7 @@ def segmented_sortcopy(input, output, buffer, offsets, scratch, direction="ascfw
     t = tuning if tuning is not None else tuning_for(d.key_bytes)
     nsegs = int(offsets.numel()) - 1
     api._check(_lib().rsbd8g_segmented_sortcopy(
-        ctypes.byref(d), int(input.numel()), nsegs, api._ptr(offsets), api._ptr(scratch),
+        ctypes.byref(d), api._count(input, None, d), nsegs, api._ptr(offsets), api._ptr(scratch),
         scratch.numel() * scratch.element_size(), api._ptr(input), api._ptr(output), api._ptr(buffer),
         ctypes.byref(t), api._stream(stream)), "rsbd8g_segmented_sortcopy")
 
@@ -117,7 +132,8 @@ class SegmentedSorter:
         self.tuning = tuning if tuning is not None else tuning_for(api.key_kind(self.key_dtype)[1])
         self.output = torch.empty_like(input)
         self.buffer = torch.empty_like(input)
-        nb = segmented_scratch_bytes(self.key_dtype, int(input.numel()), int(offsets.numel()) - 1,
+        total = int(input.numel() * input.element_size() // api.key_kind(self.key_dtype)[1])
+        nb = segmented_scratch_bytes(self.key_dtype, total, int(offsets.numel()) - 1,
                                      direction, mode, self.tuning)
         self.scratch = torch.empty(nb, dtype=torch.uint8, device=input.device)
         self.stream = stream if stream is not None else torch.cuda.Stream(device=input.device)

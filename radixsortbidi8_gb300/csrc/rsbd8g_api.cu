@@ -192,6 +192,12 @@ Layout layout_for(const Resolved &r, uint64_t n) {
     return L;
 }
 
+int filter_class(const rsbd8g_desc *d) {
+    Resolved r;
+    if (resolve(d, &r) != RSBD8G_OK) return -1;
+    return int(r.f.absv | (r.f.sign << 1) | (r.f.fltp << 2) | (r.x87 << 3));
+}
+
 bool device_memory(const void *p) {
     if (!p) return true;                  // an absent array takes no part
     cudaPointerAttributes at{};
@@ -340,6 +346,46 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc(const rsbd8g_desc *desc, size_t
                    ? RSBD8G_OK : RSBD8G_ERR_CUDA;
     }
     if (!buffer || buffer == input) return RSBD8G_ERR_BAD_ARG;
+    return enqueue_sort(r, count, scratch, scratch_bytes, input, nullptr, buffer, true, movetobuffer != 0, s);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortcopynoalloc_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                           void *scratch, size_t scratch_bytes, const void *input,
+                                                           void *output, void *buffer, rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (r.indirect != RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
+    r.keys = keys;
+    if (count == 0) return RSBD8G_OK;
+    if (!input || !output || input == output) return RSBD8G_ERR_BAD_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (count == 1) {
+        return cudaMemcpyAsync(output, input, r.elem_bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+    }
+    if (!keys || !buffer || buffer == input || buffer == output) return RSBD8G_ERR_BAD_ARG;
+    return enqueue_sort(r, count, scratch, scratch_bytes, input, output, buffer, false, false, s);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_radixsortnoalloc_keyed(const rsbd8g_desc *desc, size_t count, const void *keys,
+                                                       void *scratch, size_t scratch_bytes, void *input, void *buffer,
+                                                       int movetobuffer, rsbd8g_stream stream) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    if (r.indirect != RSBD8G_KEYED) return RSBD8G_ERR_BAD_ARG;
+    r.keys = keys;
+    if (count == 0) return RSBD8G_OK;
+    if (!input) return RSBD8G_ERR_BAD_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (count == 1) {
+        if (!movetobuffer) return RSBD8G_OK;
+        if (!buffer) return RSBD8G_ERR_BAD_ARG;
+        return cudaMemcpyAsync(buffer, input, r.elem_bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? RSBD8G_OK : RSBD8G_ERR_CUDA;
+    }
+    if (!keys || !buffer || buffer == input) return RSBD8G_ERR_BAD_ARG;
     return enqueue_sort(r, count, scratch, scratch_bytes, input, nullptr, buffer, true, movetobuffer != 0, s);
 }
 

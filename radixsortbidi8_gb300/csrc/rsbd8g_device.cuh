@@ -44,8 +44,12 @@ struct PassPlan {
     void *dst_vals;
     uint32_t active;
     uint32_t reverse;      // read the source back to front (isrevorder, first surviving pass)
-    uint32_t pad0, pad1;
+    uint32_t hot;          // crowded digits of the pass, ranked with ballots: (digit1 << 16) | digit0,
+                           // kNoHot in a half for none (see TileRank)
+    uint32_t pad1;
 };
+constexpr uint32_t kNoHot = 0x100u;                       // not a digit: matches no key
+constexpr uint32_t kNoHotPair = (kNoHot << 16) | kNoHot;
 
 struct Control {
     uint32_t error;
@@ -70,7 +74,7 @@ static_assert(sizeof(Control) <= 1024, "control block must fit its slot");
 // (the low three bits of the resolved sortingmode).  Descending sorts use the complement ~K,
 // which the kernels apply per digit.
 template <int MODE, typename U>
-__device__ __forceinline__ U filter_key(U b) {
+__host__ __device__ __forceinline__ U filter_key(U b) {
     constexpr bool ABS = (MODE & 1) != 0, SIGN = (MODE & 2) != 0, FLTP = (MODE & 4) != 0;
     constexpr int W = int(sizeof(U)) * 8;
     constexpr U sb = U(U(1) << (W - 1));
@@ -125,9 +129,9 @@ template <int HB> struct KeyTraits<KeyWide<HB>> {
 
 // the complement of a filtered key (descending order), within the key's bits
 template <typename U>
-__device__ __forceinline__ U key_not(U k) { return U(~k); }
+__host__ __device__ __forceinline__ U key_not(U k) { return U(~k); }
 template <int HB>
-__device__ __forceinline__ KeyWide<HB> key_not(KeyWide<HB> k) {
+__host__ __device__ __forceinline__ KeyWide<HB> key_not(KeyWide<HB> k) {
     return KeyWide<HB>{~k.lo, ~k.hi & KeyWide<HB>::kHighMask};
 }
 
@@ -139,7 +143,7 @@ __device__ __forceinline__ uint32_t digit_of(KeyWide<HB> k, int pass) {
 // K(b) of the same 8 filter combinations on the (64 + HB)-bit key; the result keeps `hi` within
 // HB bits, so the padding of an x87 key never reaches a digit
 template <int MODE, int HB>
-__device__ __forceinline__ KeyWide<HB> filter_key(KeyWide<HB> b) {
+__host__ __device__ __forceinline__ KeyWide<HB> filter_key(KeyWide<HB> b) {
     using K = KeyWide<HB>;
     constexpr bool ABS = (MODE & 1) != 0, SIGN = (MODE & 2) != 0, FLTP = (MODE & 4) != 0;
     constexpr uint64_t hm = K::kHighMask, sb = uint64_t(1) << (HB - 1);

@@ -86,7 +86,9 @@ constexpr SweepGeometry sweep_geometry_small(int key_bytes) {
 // the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
 // segment's last tile is partly empty, and large 8-byte segments are the shorter ones); keys up to
 // 4 bytes take 512 x 28 (measured against 24 and 32 on the 2^28-key batch of uint32 arrays)
-constexpr SweepGeometry seg_sweep_geometry(int key_bytes) { return SweepGeometry{512, key_bytes == 8 ? 12 : 28}; }
+constexpr SweepGeometry seg_sweep_geometry(int key_bytes) {
+    return SweepGeometry{512, key_bytes == 16 ? 6 : (key_bytes == 8 ? 12 : 28)};
+}
 
 #define RSBD8G_MODE_SWITCH(mode, CALL) \
     switch (mode) {                    \
@@ -105,7 +107,8 @@ struct SegSmallShape {
     int threads, items;
 };
 constexpr SegSmallShape seg_small_shape(int key_bytes, int variant) {
-    return key_bytes == 8 ? (variant == 0 ? SegSmallShape{256, 8} : variant == 1 ? SegSmallShape{256, 12} : SegSmallShape{512, 12})
+    return key_bytes == 16 ? (variant == 0 ? SegSmallShape{256, 4} : variant == 1 ? SegSmallShape{256, 6} : SegSmallShape{512, 4})
+         : key_bytes == 8 ? (variant == 0 ? SegSmallShape{256, 8} : variant == 1 ? SegSmallShape{256, 12} : SegSmallShape{512, 12})
                           : (variant == 0 ? SegSmallShape{256, 8} : variant == 1 ? SegSmallShape{256, 16} : SegSmallShape{512, 16});
 }
 constexpr int kSegSmallVariants = 3;
@@ -125,10 +128,14 @@ RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k1)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k2)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k4)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k8)
+RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k16)
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
 // p is device memory (cudaMalloc, a memory pool, a __device__ array); null counts as such
 bool device_memory(const void *p);
+// the resolved filter of a descriptor (isabsvalue | issignmode << 1 | isfltpmode << 2 | x87 << 3),
+// -1 for a bad descriptor: descriptors of one key size and filter sort alike but for direction
+int filter_class(const rsbd8g_desc *d);
 Layout layout_for(const Resolved &r, uint64_t n);
 rsbd8g_status enqueue_sort(const Resolved &r, uint64_t n, void *scratch, size_t scratch_bytes, const void *in,
                            void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);

@@ -191,18 +191,49 @@ struct PlanArgs {
     uint32_t stall_tile;
     uint32_t passes;       // digits of the key
     uint32_t prefetch;     // every array is device memory (Control::prefetch)
+    uint32_t hot_ok;       // crowded digits may be ranked with ballots (PassPlan::hot)
 };
+
+// a digit is ranked with ballots (PassPlan::hot) when it holds more than 1/kHotShare of the keys: the
+// ballots cost every key of the pass instructions (about 30 % more time on a pass of uniform digits
+// with two hot digits), and they pay only where many lanes of a unit share the digit (float32 keys
+// of N(0, 1e3) by absolute value, top digit: 56 % of the keys in one bucket, 28 % in the next; that
+// pass 1.13 ms -> 1.05 ms at 2^28 keys with the fullest digit ranked by ballots, 1.13 ms with both)
+constexpr unsigned long long kHotShare = 4;
+
+// the largest value over the 256 threads of k_plan (all threads call it)
+__device__ __forceinline__ unsigned long long plan_block_max(unsigned long long v, unsigned long long *wbuf) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = y > v ? y : v;
+    }
+    if (lane == 0) wbuf[w] = v;
+    __syncthreads();
+    unsigned long long m = wbuf[0];
+    for (int i = 1; i < 8; ++i) m = wbuf[i] > m ? wbuf[i] : m;
+    __syncthreads();
+    return m;
+}
 
 // one CTA of 256 threads
 static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
                                               unsigned long long *__restrict__ bstart, uint64_t n, PlanArgs a) {
     __shared__ unsigned long long wsum[8];
     __shared__ int skip[kMaxPasses];
+    __shared__ uint32_t hot[kMaxPasses];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     for (int p = 0; p < int(a.passes); ++p) {
         const unsigned long long h = ghist[p * kBuckets + t];
         // pass-skip: one bucket holds every key (Radixsortbidi8.hpp:12259, :12272, :2903)
         const int all_in_one = __syncthreads_or(h == n);
+        // the pass's fullest bucket, (count << 8) | digit: a crowded one is ranked with ballots
+        const unsigned long long m0 = plan_block_max((h << 8) | uint32_t(t), wsum);
+        if (t == 0) {
+            const uint32_t h0 = (m0 >> 8) > n / kHotShare ? uint32_t(m0 & 0xFFu) : kNoHot;
+            hot[p] = a.hot_ok ? ((kNoHot << 16) | h0) : kNoHotPair;
+        }
         unsigned long long x = h;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -232,6 +263,7 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
     for (int p = 0; p < int(a.passes); ++p) {
         PassPlan &pp = ctrl->plan[p];
         pp.active = !skip[p];
+        pp.hot = hot[p];
         if (skip[p]) continue;
         ++i;
         void *dst;
@@ -317,6 +349,12 @@ __device__ __forceinline__ uint32_t pass_digit(U k, int pass, uint32_t dmask) {
 // Both tables take (THREADS / 16) * 256 words.  A unit holds at most LANES * ITEMS keys, so counts
 // stay below 2^16.  Large tiles keep their ranks two to a register and recompute the digit when the
 // key is staged (registers are what limits them); small tiles keep (rank << 8) | digit per key.
+//   Crowded passes (HOT > 0): up to two digits that hold a large share of the pass's keys (found in
+// the pass's histogram) never touch the table while ranking -- many lanes of a unit holding the same
+// digit would serialise on one word.  For those digits a ballot gives the unit's peers, each unit
+// keeps the digit's running count in a register (the same value in all its lanes), and the unit's
+// first lane stores the count into the table word afterwards, where the scan finds it: the ranks
+// are the ones the table would have given.
 
 template <int MODE, typename U>
 __device__ __forceinline__ uint32_t slot_digit(const U &k, uint32_t slot, uint32_t tvalid, int pass, uint32_t dmask) {
@@ -341,44 +379,77 @@ struct TileRank {
     // the unit's count (later offset) words
     __device__ static uint32_t *row(uint32_t *tab) { return tab + (threadIdx.x / LANES) * kBuckets; }
 
-    // rank this lane's ITEMS keys within its unit (the unit's masks clear, its counts zero)
-    template <int MODE, typename U>
+    // rank this lane's ITEMS keys within its unit (the unit's masks clear, its counts zero); with
+    // HOT > 0 the digits in `hot` ((digit1 << 16) | digit0, kNoHot for none) are ranked by ballots
+    template <int MODE, int HOT = 0, typename U>
     __device__ static void rank(const U (&keys)[ITEMS], uint32_t (&rk)[kRankRegs], uint32_t *tab, uint32_t slot0,
-                                uint32_t tvalid, int pass, uint32_t dmask) {
+                                uint32_t tvalid, int pass, uint32_t dmask, uint32_t hot = kNoHotPair) {
         uint32_t *crow = row(tab);
         const uint32_t bit = 1u << (threadIdx.x % LANES), below = bit - 1u;
+        // this unit's lanes within a warp ballot
+        const uint32_t ushift = LANES == 16 ? (threadIdx.x & 16u) : 0u;
+        const uint32_t umask = LANES == 16 ? 0xFFFFu : 0xFFFFFFFFu;
+        const uint32_t h0 = hot & 0xFFFFu, h1 = hot >> 16;
+        uint32_t hc0 = 0, hc1 = 0;          // the unit's running counts of the hot digits
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
             const uint32_t d = slot_digit<MODE>(keys[i], slot0 + uint32_t(LANES) * i, tvalid, pass, dmask);
+            bool is_hot = false;
+            uint32_t rh = 0;
+            if constexpr (HOT > 0) {
+                const uint32_t b0 = (__ballot_sync(0xFFFFFFFFu, d == h0) >> ushift) & umask;
+                if (d == h0) {
+                    rh = hc0 + uint32_t(__popc(b0 & below));
+                    is_hot = true;
+                }
+                hc0 += uint32_t(__popc(b0));
+                if constexpr (HOT > 1) {
+                    const uint32_t b1 = (__ballot_sync(0xFFFFFFFFu, d == h1) >> ushift) & umask;
+                    if (d == h1) {
+                        rh = hc1 + uint32_t(__popc(b1 & below));
+                        is_hot = true;
+                    }
+                    hc1 += uint32_t(__popc(b1));
+                }
+            }
             uint32_t r;
             if constexpr (LANES == 16) {
-                atomicOr(crow + d, bit);
+                if (!is_hot) atomicOr(crow + d, bit);
                 __syncwarp();
-                const uint32_t w = crow[d];
+                const uint32_t w = is_hot ? 0u : crow[d];
                 __syncwarp();
                 const uint32_t peers = w & 0xFFFFu;
                 const uint32_t lower = uint32_t(__popc(peers & below));
-                if (lower == 0) atomicAdd(crow + d, (uint32_t(__popc(peers)) << 16) - peers);
+                if (!is_hot && lower == 0) atomicAdd(crow + d, (uint32_t(__popc(peers)) << 16) - peers);
                 __syncwarp();      // the cleared mask is visible to the next item's updates
-                r = (w >> 16) + lower;
+                r = is_hot ? rh : (w >> 16) + lower;
             } else {
                 uint32_t *mrow = tab + (THREADS / 32) * kBuckets + (threadIdx.x / 32) * kBuckets;
-                atomicOr(mrow + d, bit);
+                if (!is_hot) atomicOr(mrow + d, bit);
                 __syncwarp();
-                const uint32_t peers = mrow[d];
+                const uint32_t peers = is_hot ? 0u : mrow[d];
                 __syncwarp();
                 const uint32_t lower = uint32_t(__popc(peers & below));
                 uint32_t before = 0;
-                if (lower == 0) {
+                if (!is_hot && lower == 0) {
                     before = atomicAdd(crow + d, uint32_t(__popc(peers)));
                     mrow[d] = 0u;
                 }
                 __syncwarp();
-                r = __shfl_sync(0xFFFFFFFFu, before, __ffs(peers) - 1) + lower;
+                const uint32_t src = peers ? uint32_t(__ffs(peers) - 1) : 0u;
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, before, src);
+                r = is_hot ? rh : b + lower;
             }
             if constexpr (!kPacked) rk[i] = (r << 8) | d;
             else if (i & 1) rk[i >> 1] |= r << 16;
             else rk[i >> 1] = r;
+        }
+        if constexpr (HOT > 0) {
+            // the hot digits' unit counts go where the table keeps counts (their words are zero)
+            if (threadIdx.x % LANES == 0) {
+                if (h0 < kBuckets) crow[h0] = hc0 << kShift;
+                if (HOT > 1 && h1 < kBuckets) crow[h1] = hc1 << kShift;
+            }
         }
     }
 
@@ -555,11 +626,11 @@ struct SweepTile {
 // Process one tile: load, rank (half-warp multisplit), publish and resolve the look-back, stage sorted
 // by digit in shared memory, write out.  `bstart` (shared) holds the bucket starts of this pass for
 // the array / segment.  Called by all threads; ends with a barrier.
-template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S, int HOT = 0>
 __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<U, S> &t,
                                            const unsigned long long *bstart, int pass, uint32_t dmask,
                                            uint32_t *err_word, uint32_t *abort_word, uint64_t spin_limit,
-                                           uint32_t stall_tile) {
+                                           uint32_t stall_tile, uint32_t hot = kNoHotPair) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     constexpr int TILE = L::kTile;
     using R = TileRank<THREADS, ITEMS>;
@@ -583,7 +654,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     const uint32_t slot0 = R::slot0();
     load_items<ITEMS, R::kLanes>(keys, t.src_k, n, tbase, slot0, tvalid, TILE, t.reverse, KeyTraits<U>::fill());
     if constexpr (HAS_VAL) load_items<ITEMS, R::kLanes>(vals, t.src_v, n, tbase, slot0, tvalid, TILE, t.reverse, uint64_t(0));
-    R::template rank<MODE>(keys, rk, wofs, slot0, tvalid, pass, dmask);
+    R::template rank<MODE, HOT>(keys, rk, wofs, slot0, tvalid, pass, dmask, hot);
     __syncthreads();
 
     // per digit: the tile count; publish the aggregate
@@ -675,19 +746,14 @@ __device__ __forceinline__ void sweep_init_smem(unsigned char *smem) {
     for (int i = threadIdx.x; i < (THREADS / 16) * kBuckets; i += THREADS) wofs[i] = 0u;
 }
 
-template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
-__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
-    k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
-               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S, int HOT>
+__device__ __forceinline__ void onesweep_body(unsigned char *smem, Control *__restrict__ ctrl,
+                                              const PassPlan &plan, const unsigned long long *__restrict__ bstart_all,
+                                              S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles,
+                                              uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
-    static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
-    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
-    extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);
-
-    const PassPlan plan = ctrl->plan[pass];
-    if (!plan.active) return;
     SweepTile<U, S> t;
     t.src_k = static_cast<const U *>(plan.src_keys);
     t.dst_k = static_cast<U *>(plan.dst_keys);
@@ -718,9 +784,26 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
         const uint32_t tile = misc[0];
         if (tile >= num_tiles) break;
         t.tile = tile;
-        sweep_tile<U, MODE, HAS_VAL, THREADS, ITEMS, S>(smem, t, bstart, pass, dmask, &ctrl->error, &ctrl->abort,
-                                                        spin_limit, stall_tile);
+        sweep_tile<U, MODE, HAS_VAL, THREADS, ITEMS, S, HOT>(smem, t, bstart, pass, dmask, &ctrl->error,
+                                                             &ctrl->abort, spin_limit, stall_tile, plan.hot);
     }
+}
+
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+__global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
+    k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
+               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+    using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
+    static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
+    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PassPlan plan = ctrl->plan[pass];
+    if (!plan.active) return;
+    // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
+    if (plan.hot == kNoHotPair)
+        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, bstart_all, status, pass, n, num_tiles, dmask);
+    else
+        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, bstart_all, status, pass, n, num_tiles, dmask);
 }
 
 // ---- the pipelined scatter pass -----------------------------------------------------------------
@@ -750,16 +833,15 @@ struct PipeSmem {
     static constexpr size_t kBytes = kOffHalf + 2 * kBuckets * 4;
 };
 
-template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
-__global__ void __launch_bounds__(THREADS, 2)
-    k_onesweep_pipe(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
-                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
-    static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S, int HOT>
+__device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control *__restrict__ ctrl, const PassPlan &plan,
+                                                   const unsigned long long *__restrict__ bstart_all,
+                                                   S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles,
+                                                   uint32_t dmask) {
     using L = PipeSmem<U, THREADS, ITEMS, HAS_VAL>;
-    static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
     using R = TileRank<THREADS, ITEMS>;
-    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t hot = plan.hot;
     U *stage = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
@@ -773,8 +855,6 @@ __global__ void __launch_bounds__(THREADS, 2)
     constexpr bool kSplit = R::kUnits == 32;
     uint32_t *half = reinterpret_cast<uint32_t *>(smem + L::kOffHalf);
 
-    const PassPlan plan = ctrl->plan[pass];
-    if (!plan.active) return;
     const U *src = static_cast<const U *>(plan.src_keys);
     U *dst = static_cast<U *>(plan.dst_keys);       // null: keys are dropped (last pass of an indirect sort)
     const uint64_t *src_v = static_cast<const uint64_t *>(plan.src_vals);
@@ -828,7 +908,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
             load_items<ITEMS, R::kLanes>(keys, src, n, tbase, slot0, tvalidB, TILE, reverse, KeyTraits<U>::fill());
             if constexpr (HAS_VAL) load_items<ITEMS, R::kLanes>(vals, src_v, n, tbase, slot0, tvalidB, TILE, reverse, uint64_t(0));
-            R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, dmask);
+            R::template rank<MODE, HOT>(keys, rk, utab, slot0, tvalidB, pass, dmask, hot);
         }
         __syncthreads();                                                        // barrier 1
 
@@ -949,6 +1029,24 @@ __global__ void __launch_bounds__(THREADS, 2)
         par ^= 1;
         tileB = hasB ? misc[0] : num_tiles;
     }
+}
+
+template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
+__global__ void __launch_bounds__(THREADS, 2)
+    k_onesweep_pipe(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
+                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+    static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
+    static_assert(PipeSmem<U, THREADS, ITEMS, HAS_VAL>::kTile <= 65535, "tile ranks are 16-bit");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PassPlan plan = ctrl->plan[pass];
+    if (!plan.active) return;
+    // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
+    if (plan.hot == kNoHotPair)
+        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, bstart_all, status, pass, n,
+                                                                   num_tiles, dmask);
+    else
+        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, bstart_all, status, pass, n,
+                                                                   num_tiles, dmask);
 }
 
 

@@ -118,6 +118,7 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     a.indirect = r.indirect != 0;
     a.passes = uint32_t(KeyTraits<U>::kDigits);
     a.prefetch = r.prefetch;
+    a.hot_ok = 1u;
     const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
     a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
     a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;

@@ -62,7 +62,7 @@ cudaError_t launch_seg_sweeps_t(const SegArgs &a, const SegLayout &L, unsigned c
     const uint64_t resident = pipe ? president : uint64_t(occ[dev & 63]) * device_sms(dev);
     const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(L.tiles_max, resident)));
     uint32_t *status = reinterpret_cast<uint32_t *>(scratch + L.status);
-    for (int p = 0; p < int(sizeof(U)); ++p) {
+    for (int p = 0; p < KeyTraits<U>::kDigits; ++p) {
         cudaError_t e;
         {
             LaunchTimer t(s, RSBD8G_KERNEL_MEMSET, uint32_t(sizeof(U)), uint32_t(p), L.tiles_max);
@@ -71,9 +71,9 @@ cudaError_t launch_seg_sweeps_t(const SegArgs &a, const SegLayout &L, unsigned c
         if (e != cudaSuccess) return e;
         LaunchTimer t(s, RSBD8G_KERNEL_SEGMENTED, uint32_t(sizeof(U)), uint32_t(p), L.tiles_max);
         if (pipe)
-            pkern<<<grid, THREADS, PM::kBytes, s>>>(a, p, int(sizeof(U)), in, out, buf, status, stall_tile);
+            pkern<<<grid, THREADS, PM::kBytes, s>>>(a, p, KeyTraits<U>::kDigits, in, out, buf, status, stall_tile);
         else
-            kern<<<grid, THREADS, SM::kBytes, s>>>(a, p, int(sizeof(U)), in, out, buf, status, stall_tile);
+            kern<<<grid, THREADS, SM::kBytes, s>>>(a, p, KeyTraits<U>::kDigits, in, out, buf, status, stall_tile);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -104,7 +104,8 @@ cudaError_t launch_segmented_mode_t(const Resolved &r, const SegArgs &a, const S
     if (e != cudaSuccess) return e;
     {
         LaunchTimer t(s, RSBD8G_KERNEL_HISTOGRAM, uint32_t(sizeof(U)), 0, a.nsegs);
-        constexpr size_t smem = size_t(hist_lane_copies<int(sizeof(U))>()) * sizeof(U) * kBuckets * 4;
+        constexpr int P = KeyTraits<U>::kDigits;
+        constexpr size_t smem = size_t(hist_lane_copies<P>()) * P * kBuckets * 4;
         auto kern = k_seg_hist<U, MODE, 1024>;
         static std::once_flag once[64];
         std::call_once(once[dev & 63],
@@ -115,7 +116,7 @@ cudaError_t launch_segmented_mode_t(const Resolved &r, const SegArgs &a, const S
     {
         LaunchTimer t(s, RSBD8G_KERNEL_PLAN, uint32_t(sizeof(U)), 0, a.nsegs);
         const uint32_t g = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(a.nlarge_max, uint64_t(sms) * 16)));
-        k_seg_plan<<<g, 256, 0, s>>>(a, int(sizeof(U)));
+        k_seg_plan<<<g, 256, 0, s>>>(a, KeyTraits<U>::kDigits);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     constexpr SweepGeometry gd = seg_sweep_geometry(int(sizeof(U)));

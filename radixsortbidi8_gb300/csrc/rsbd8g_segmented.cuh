@@ -52,7 +52,19 @@ struct SegArgs {
     const uint64_t *ptr_buf;
     uint64_t spin_limit_ns;   // bound of every look-back wait
     uint32_t prefetch;        // every array is device memory: tiles may be prefetched into L2
+    // per-segment directions (sortingdirection values, one byte per segment); null: dmask and rev
+    // above hold for every segment.  rev_ok: the mode honours isrevorder (a uniform property)
+    const uint8_t *seg_dir;
+    uint32_t rev_ok;
 };
+
+// the digit complement (descending sorts) and the effective isrevorder of segment `seg`
+__device__ __forceinline__ uint32_t seg_dmask(const SegArgs &a, uint32_t seg) {
+    return a.seg_dir ? ((a.seg_dir[seg] & 1u) ? 0xFFu : 0u) : a.dmask;
+}
+__device__ __forceinline__ bool seg_rev(const SegArgs &a, uint32_t seg) {
+    return a.seg_dir ? (((a.seg_dir[seg] >> 1) & 1u) != 0 && a.rev_ok != 0) : a.rev != 0;
+}
 
 __device__ __forceinline__ uint64_t seg_len(const uint64_t *off, uint32_t s) { return off[s + 1] - off[s]; }
 
@@ -149,7 +161,7 @@ __device__ __forceinline__ uint32_t seg_of_tile(const uint32_t *tbase, uint32_t 
 // (and records the segment of each of those tiles for the scatter passes)
 template <typename U, int MODE, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__restrict__ in) {
-    constexpr int P = int(sizeof(U));
+    constexpr int P = KeyTraits<U>::kDigits;
     constexpr int C = hist_lane_copies<P>();
     extern __shared__ __align__(16) uint32_t shl[];   // C lane-class copies, as in k_histogram
     const SegControl *c = a.ctrl;
@@ -168,6 +180,7 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         const uint32_t seg = a.large_seg[idx];
         const uint64_t len = seg_len(a.offsets, seg);
         const U *src = seg_ptr(a, a.ptr_in, in, seg);
+        const uint32_t dm = seg_dmask(a, seg);
         const uint32_t tend = min(t1, a.large_tbase[idx + 1]);
         for (uint32_t x = gt + threadIdx.x; x < tend; x += THREADS) a.tile_seg[x] = idx;
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
@@ -178,14 +191,14 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 const uint64_t i = b + uint64_t(u) * THREADS;
-                raw[u] = i < k1 ? src[i] : U(0);
+                raw[u] = i < k1 ? src[i] : U{};
             }
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 if (b + uint64_t(u) * THREADS >= k1) break;
                 const U k = filter_key<MODE>(raw[u]);
 #pragma unroll
-                for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ a.dmask)) * C, 1u);
+                for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dm)) * C, 1u);
             }
         }
         __syncthreads();
@@ -284,8 +297,8 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, false, THREADS
         t.status = status + size_t(a.large_tbase[idx]) * kBuckets;
         t.n = len;
         t.tile = gt - a.large_tbase[idx];
-        t.reverse = a.rev && i == 1;
-        sweep_tile<U, MODE, false, THREADS, ITEMS, uint32_t>(smem, t, bstart, pass, a.dmask, &c->error, &c->abort,
+        t.reverse = seg_rev(a, seg) && i == 1;
+        sweep_tile<U, MODE, false, THREADS, ITEMS, uint32_t>(smem, t, bstart, pass, seg_dmask(a, seg), &c->error, &c->abort,
                                                              spin_limit, stall_tile);
     }
 }
@@ -303,6 +316,7 @@ struct SegPipeTile {
     uint64_t n;                // keys of the segment
     uint32_t tile;             // tile index within the segment
     uint32_t reverse;
+    uint32_t dmask;            // the segment's digit complement (descending sorts)
 };
 
 template <typename U>
@@ -322,7 +336,8 @@ __device__ __forceinline__ bool seg_pipe_tile(const SegArgs &a, int pass, int pa
     t.status = status + size_t(a.large_tbase[idx]) * kBuckets;
     t.n = seg_len(a.offsets, seg);
     t.tile = gt - a.large_tbase[idx];
-    t.reverse = (a.rev && i == 1) ? 1u : 0u;
+    t.reverse = (seg_rev(a, seg) && i == 1) ? 1u : 0u;
+    t.dmask = seg_dmask(a, seg);
     return true;
 }
 
@@ -397,7 +412,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             const uint64_t tbase = uint64_t(B.tile) * TILE;
             tvalidB = uint32_t((n - tbase) < uint64_t(TILE) ? (n - tbase) : uint64_t(TILE));
             load_items<ITEMS, R::kLanes>(keys, src, n, tbase, slot0, tvalidB, TILE, B.reverse != 0, KeyTraits<U>::fill());
-            R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, a.dmask);
+            R::template rank<MODE>(keys, rk, utab, slot0, tvalidB, pass, B.dmask);
         }
         __syncthreads();                                                        // barrier 1
 
@@ -447,7 +462,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             const uint64_t n = A.n;
             for (uint32_t s = tid; s < tvalidA; s += THREADS) {
                 const U k = stage[s];
-                const long long g = gofs[pass_digit<MODE>(k, pass, a.dmask)] + (long long)s;
+                const long long g = gofs[pass_digit<MODE>(k, pass, A.dmask)] + (long long)s;
                 if (uint64_t(g) < n) dst[g] = k;
                 else atomicOr(err_word, kDevFault);     // an offset outside the segment: flagged, not written
             }
@@ -457,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         if (hasB) {
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalidB, pass, a.dmask);
+                const uint32_t d = R::template digit_of_item<MODE>(rk, i, keys[i], slot0 + uint32_t(R::kLanes) * i, tvalidB, pass, B.dmask);
                 stage[urow[d] + R::rank_of(rk, i)] = keys[i];
             }
             R::clear_own(utab);
@@ -493,7 +508,8 @@ __global__ void __launch_bounds__(256) k_seg_copy(SegArgs a, const U *__restrict
         const uint64_t len = seg_len(a.offsets, seg);
         const U *src = seg_ptr(a, a.ptr_in, in, seg);
         U *dst = seg_ptr(a, a.ptr_out, out, seg);
-        for (uint64_t i = lane; i < len; i += 32) dst[i] = src[a.rev ? len - 1 - i : i];
+        const bool rev = seg_rev(a, seg);
+        for (uint64_t i = lane; i < len; i += 32) dst[i] = src[rev ? len - 1 - i : i];
     }
 }
 
@@ -515,7 +531,7 @@ struct SmallSmem {
 template <typename U, int MODE, int THREADS, int ITEMS>
 __global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__restrict__ in, U *__restrict__ out) {
     using L = SmallSmem<U, THREADS, ITEMS>;
-    constexpr int P = int(sizeof(U));
+    constexpr int P = KeyTraits<U>::kDigits;
     constexpr int WARPS = L::kWarps;
     constexpr int ST = L::kStride;
     static_assert(THREADS >= kBuckets, "one thread per digit");
@@ -543,7 +559,9 @@ __global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__res
         const uint32_t len = uint32_t(seg_len(a.offsets, seg));
         const U *sin = seg_ptr(a, a.ptr_in, in, seg);
         U *sout = seg_ptr(a, a.ptr_out, out, seg);
-        for (uint32_t i = tid; i < len; i += THREADS) A[i] = sin[a.rev ? len - 1u - i : i];
+        const bool rev = seg_rev(a, seg);
+        const uint32_t dm = seg_dmask(a, seg);
+        for (uint32_t i = tid; i < len; i += THREADS) A[i] = sin[rev ? len - 1u - i : i];
         // warp w ranks slots [w * chunk, min((w + 1) * chunk, len)) in steps of 32
         const uint32_t chunk = ((len + WARPS - 1) / WARPS + 31u) & ~31u;
         const uint32_t w0 = min(len, uint32_t(warp) * chunk), w1 = min(len, w0 + chunk);
@@ -555,7 +573,7 @@ __global__ void __launch_bounds__(THREADS) k_seg_small(SegArgs a, const U *__res
             for (uint32_t b = w0; b < w1; b += 32) {
                 const uint32_t slot = b + uint32_t(lane);
                 const bool ok = slot < w1;
-                const uint32_t d = ok ? pass_digit<MODE>(src[slot], p, a.dmask) : uint32_t(kBuckets);
+                const uint32_t d = ok ? pass_digit<MODE>(src[slot], p, dm) : uint32_t(kBuckets);
                 atomicOr(wmask + d, 1u << lane);
                 __syncwarp();
                 const uint32_t peers = wmask[d];

@@ -29,7 +29,7 @@ rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, cons
     L->nlarge_max = std::max<uint64_t>(1, std::min<uint64_t>(nsegs, total / (uint64_t(cutoff) + 1)));
     L->tiles_max = total / L->tile + L->nlarge_max + 1;
     if (L->tiles_max >= (uint64_t(1) << 32) || nsegs >= (uint64_t(1) << 32)) return RSBD8G_ERR_TOO_LARGE;
-    const uint64_t P = r.key_bytes;
+    const uint64_t P = r.digits;
     L->ctrl = 0;
     L->seg_hist = up(sizeof(SegControl));
     L->zero_bytes = L->seg_hist + up(L->nlarge_max * P * kBuckets * 4);
@@ -56,7 +56,7 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc,
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
-    if (r.indirect != RSBD8G_DIRECT || !bytes || r.key_bytes == 16) return RSBD8G_ERR_BAD_ARG;
+    if (r.indirect != RSBD8G_DIRECT || !bytes || r.x87) return RSBD8G_ERR_BAD_ARG;
     SegLayout L;
     if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
     *bytes = L.total;
@@ -66,11 +66,12 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc,
 static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, size_t nsegs, const uint64_t *offsets,
                                       void *scratch, size_t scratch_bytes, const void *input, void *output,
                                       void *buffer, const uint64_t *in_ptrs, const uint64_t *out_ptrs,
-                                      const uint64_t *buf_ptrs, const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
+                                      const uint64_t *buf_ptrs, const uint8_t *seg_dirs, const rsbd8g_segtuning *tuning,
+                                      rsbd8g_stream stream) {
     Resolved r;
     rsbd8g_status st = resolve(desc, &r);
     if (st != RSBD8G_OK) return st;
-    if (r.indirect != RSBD8G_DIRECT || r.key_bytes == 16) return RSBD8G_ERR_BAD_ARG;
+    if (r.indirect != RSBD8G_DIRECT || r.x87) return RSBD8G_ERR_BAD_ARG;
     if (nsegs == 0 || total == 0) return RSBD8G_OK;
     if (!offsets || !scratch) return RSBD8G_ERR_BAD_ARG;
     if (!in_ptrs) {
@@ -80,6 +81,10 @@ static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, siz
         return RSBD8G_ERR_BAD_ARG;
     }
     if ((reinterpret_cast<uintptr_t>(scratch) & (kA - 1)) != 0) return RSBD8G_ERR_BAD_ARG;
+    if (r.key_bytes == 16 && !in_ptrs) {      // 16-byte keys move as aligned 16-byte words
+        auto mis = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; };
+        if (mis(input) || mis(output) || mis(buffer)) return RSBD8G_ERR_BAD_ARG;
+    }
     SegLayout L;
     if ((st = seg_layout(r, total, nsegs, tuning, &L)) != RSBD8G_OK) return st;
     if (scratch_bytes < L.total) return RSBD8G_ERR_BAD_ARG;
@@ -113,13 +118,18 @@ static rsbd8g_status segmented_common(const rsbd8g_desc *desc, size_t total, siz
     a.spin_limit_ns = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 200000000ull : 1000000000ull;
     // tiles are prefetched into L2 only from device memory: the contiguous form checks its three
     // arrays, the pointer-table form relies on the caller's RSBD8G_FLAG_DEVICE_ARRAYS
+    a.seg_dir = seg_dirs;
+    // isrevorder is honoured by the regular absolute modes and regular floating point
+    // (Radixsortbidi8.hpp:59877-59904), the same for every segment of the call
+    a.rev_ok = (r.f.absv && r.f.sign) || (!r.f.absv && r.f.sign && r.f.fltp);
     a.prefetch = (r.flags & RSBD8G_FLAG_DEVICE_ARRAYS) ||
                  (!in_ptrs && device_memory(input) && device_memory(output) && device_memory(buffer));
     switch (r.key_bytes) {
         case 1: e = launch_segmented_k1(r, a, L, sc, input, output, buffer, s); break;
         case 2: e = launch_segmented_k2(r, a, L, sc, input, output, buffer, s); break;
         case 4: e = launch_segmented_k4(r, a, L, sc, input, output, buffer, s); break;
-        default: e = launch_segmented_k8(r, a, L, sc, input, output, buffer, s); break;
+        case 8: e = launch_segmented_k8(r, a, L, sc, input, output, buffer, s); break;
+        default: e = launch_segmented_k16(r, a, L, sc, input, output, buffer, s); break;
     }
     return e == cudaSuccess ? RSBD8G_OK : RSBD8G_ERR_CUDA;
 }
@@ -129,7 +139,7 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy(const rsbd8g_desc *desc, size
                                                    const void *input, void *output, void *buffer,
                                                    const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
     return segmented_common(desc, total, nsegs, offsets, scratch, scratch_bytes, input, output, buffer, nullptr,
-                            nullptr, nullptr, tuning, stream);
+                            nullptr, nullptr, nullptr, tuning, stream);
 }
 
 RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs(const rsbd8g_desc *desc, size_t total, size_t nsegs,
@@ -138,7 +148,18 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs(const rsbd8g_desc *desc,
                                                         void *scratch, size_t scratch_bytes,
                                                         const rsbd8g_segtuning *tuning, rsbd8g_stream stream) {
     return segmented_common(desc, total, nsegs, offsets, scratch, scratch_bytes, nullptr, nullptr, nullptr,
-                            input_ptrs, output_ptrs, buffer_ptrs, tuning, stream);
+                            input_ptrs, output_ptrs, buffer_ptrs, nullptr, tuning, stream);
+}
+
+RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs_dirs(const rsbd8g_desc *desc, size_t total, size_t nsegs,
+                                                             const uint64_t *offsets, const uint64_t *input_ptrs,
+                                                             const uint64_t *output_ptrs, const uint64_t *buffer_ptrs,
+                                                             const uint8_t *directions, void *scratch,
+                                                             size_t scratch_bytes, const rsbd8g_segtuning *tuning,
+                                                             rsbd8g_stream stream) {
+    if (!directions && nsegs && total) return RSBD8G_ERR_BAD_ARG;
+    return segmented_common(desc, total, nsegs, offsets, scratch, scratch_bytes, nullptr, nullptr, nullptr,
+                            input_ptrs, output_ptrs, buffer_ptrs, directions, tuning, stream);
 }
 
 }  // extern "C"

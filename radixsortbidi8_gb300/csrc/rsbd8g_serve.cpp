@@ -2,10 +2,10 @@
 //
 // Requests (a descriptor, a count, a device input and a device output array) arrive from any host
 // thread.  A dispatcher thread admits pending requests in arrival order while the device-memory
-// budget and the in-flight slots allow, coalesces the admitted requests that share a descriptor
-// into one batched launch (rsbd8g_segmented_sortcopy_ptrs: every request one segment, each in its
-// own arrays), and launches each batch on its own stream, so batches overlap on the device while
-// new requests keep arriving.  The budget is one device arena allocated up front: the ping-pong
+// budget and the in-flight slots allow, coalesces the admitted requests that share a key size and
+// resolved filter (any direction) into one batched launch (rsbd8g_segmented_sortcopy_ptrs_dirs:
+// every request one segment, each in its own arrays, with its own direction), and launches each
+// batch on its own stream, so batches overlap on the device while new requests keep arriving.  The budget is one device arena allocated up front: the ping-pong
 // buffers, the batch scratch and the batch's pointer tables are carved out of it and given back
 // when the batch completes, so keys and scratch stay resident and nothing is allocated per request.
 // Completion is observed with a host function queued behind each batch on its stream.
@@ -25,7 +25,8 @@
 #include "rsbd8g.h"
 
 namespace rsbd8g {
-bool device_memory(const void *p);   // rsbd8g_api.cu
+bool device_memory(const void *p);            // rsbd8g_api.cu
+int filter_class(const rsbd8g_desc *d);       // rsbd8g_api.cu
 }
 
 namespace {
@@ -95,6 +96,7 @@ struct Request {
     double t_submit = 0, t_start = 0, t_done = 0;
     int state = 0;   // 0 pending, 1 running, 2 done
     bool device = false;   // input and output are device memory
+    int group = 0;         // requests of one group sort alike but for direction (same_group)
     rsbd8g_status status = RSBD8G_OK;
 };
 
@@ -112,9 +114,11 @@ struct Batch {
     bool launch_failed = false;
 };
 
-bool same_kind(const rsbd8g_desc &a, const rsbd8g_desc &b) {
-    return a.key_bytes == b.key_bytes && a.key_kind == b.key_kind && a.mode == b.mode &&
-           a.direction == b.direction && a.flags == b.flags;
+// requests that one segmented launch can sort: the same key size, resolved filter (the kernels'
+// template mode) and flags; the direction is per segment (an unsigned key under "native" and under
+// "nativeabs" resolves to the same filter, so those share a launch too)
+bool same_group(const Request &a, const Request &b) {
+    return a.desc.key_bytes == b.desc.key_bytes && a.group == b.group && a.desc.flags == b.desc.flags;
 }
 
 struct Server {
@@ -216,12 +220,13 @@ struct Server {
             if (slot < 0) return nullptr;
             // the head request decides the descriptor of this batch; take every pending request of
             // that descriptor, in arrival order, while its buffer fits the budget
-            const rsbd8g_desc key = pending.front()->desc;
+            const Request *head = pending.front();
+            const rsbd8g_desc key = head->desc;
             std::vector<Request *> take;
             uint64_t total = 0;
             for (auto it = pending.begin(); it != pending.end() && take.size() < max_batch_requests;) {
                 Request *r = *it;
-                if (!same_kind(r->desc, key)) {
+                if (!same_group(*r, *head)) {
                     ++it;
                     continue;
                 }
@@ -237,7 +242,7 @@ struct Server {
             size_t sb = 0;
             rsbd8g_segtuning tun{1, 0, {0, 0}};
             const size_t n = take.size();
-            const size_t tb = aup((n + 1) * 8) + 3 * aup(n * 8);
+            const size_t tb = aup((n + 1) * 8) + 3 * aup(n * 8) + aup(n);
             size_t soff = 0, toff = 0;
             bool ok = rsbd8g_segmented_scratch_bytes(&key, total, n, &tun, &sb) == RSBD8G_OK &&
                       n + 1 <= slot_table_cap && arena.alloc(sb, &soff);
@@ -291,6 +296,7 @@ struct Server {
         const size_t n = b->reqs.size();
         rsbd8g_desc key = b->reqs.front()->desc;
         uint64_t *ho = b->host_tables, *hi = ho + (n + 1), *hout = hi + n, *hbuf = hout + n;
+        uint8_t *hdir = reinterpret_cast<uint8_t *>(hbuf + n);
         ho[0] = 0;
         // the buffers are in the arena (device memory): the batch may prefetch tiles into L2 when
         // every request's arrays are device memory too
@@ -302,12 +308,14 @@ struct Server {
             hi[i] = reinterpret_cast<uint64_t>(b->reqs[i]->in);
             hout[i] = reinterpret_cast<uint64_t>(b->reqs[i]->out);
             hbuf[i] = reinterpret_cast<uint64_t>(arena_base + b->reqs[i]->buf_off);
+            hdir[i] = uint8_t(b->reqs[i]->desc.direction);
         }
         unsigned char *dt = arena_base + b->tables_off;
         uint64_t *d_off = reinterpret_cast<uint64_t *>(dt);
         uint64_t *d_in = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8));
         uint64_t *d_out = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8) + aup(n * 8));
         uint64_t *d_buf = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8) + 2 * aup(n * 8));
+        uint8_t *d_dir = dt + aup((n + 1) * 8) + 3 * aup(n * 8);
         cudaStream_t s = streams[size_t(b->slot)];
         rsbd8g_segtuning tun{1, 0, {0, 0}};
         rsbd8g_status st = RSBD8G_OK;
@@ -315,12 +323,13 @@ struct Server {
         if (cudaMemcpyAsync(d_off, ho, (n + 1) * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
             cudaMemcpyAsync(d_in, hi, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
             cudaMemcpyAsync(d_out, hout, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_buf, hbuf, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            cudaMemcpyAsync(d_buf, hbuf, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_dir, hdir, n, cudaMemcpyHostToDevice, s) != cudaSuccess)
             st = RSBD8G_ERR_CUDA;
         if (st == RSBD8G_OK)
-            st = rsbd8g_segmented_sortcopy_ptrs(&key, b->keys, n, d_off, d_in, d_out, d_buf,
-                                                arena_base + b->scratch_off, b->scratch_bytes, &tun,
-                                                reinterpret_cast<rsbd8g_stream>(s));
+            st = rsbd8g_segmented_sortcopy_ptrs_dirs(&key, b->keys, n, d_off, d_in, d_out, d_buf, d_dir,
+                                                     arena_base + b->scratch_off, b->scratch_bytes, &tun,
+                                                     reinterpret_cast<rsbd8g_stream>(s));
         if (st == RSBD8G_OK &&
             cudaMemcpyAsync(b->host_err, arena_base + b->scratch_off, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
             st = RSBD8G_ERR_CUDA;
@@ -383,7 +392,7 @@ RSBD8G_API rsbd8g_status rsbd8g_server_create(size_t budget_bytes, uint32_t max_
         uint64_t *tab = nullptr;
         uint32_t *err = nullptr;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaMallocHost(reinterpret_cast<void **>(&tab), (s.slot_table_cap * 4 + 8) * 8) != cudaSuccess ||
+            cudaMallocHost(reinterpret_cast<void **>(&tab), (s.slot_table_cap * 4 + 8) * 8 + s.slot_table_cap) != cudaSuccess ||
             cudaMallocHost(reinterpret_cast<void **>(&err), 64) != cudaSuccess) {
             cudaGetLastError();
             delete h;
@@ -416,6 +425,7 @@ RSBD8G_API rsbd8g_status rsbd8g_server_submit(rsbd8g_server *h, const rsbd8g_des
     r->in = input;
     r->out = output;
     r->device = rsbd8g::device_memory(input) && rsbd8g::device_memory(output);
+    r->group = rsbd8g::filter_class(desc);
     r->t_submit = now_s();
     {
         std::lock_guard<std::mutex> g(s.mu);

@@ -53,7 +53,7 @@ class Server:
     def submit(self, input, output, direction="ascfwdorder", mode="native", key_dtype=None) -> int:
         d = api.make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode)
         rid = ctypes.c_uint64()
-        api._check(_lib().rsbd8g_server_submit(self._h, ctypes.byref(d), int(input.numel()), api._ptr(input),
+        api._check(_lib().rsbd8g_server_submit(self._h, ctypes.byref(d), api._count(input, None, d), api._ptr(input),
                                                api._ptr(output), ctypes.byref(rid)), "rsbd8g_server_submit")
         self._keep[rid.value] = (input, output)
         return rid.value

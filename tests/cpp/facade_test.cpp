@@ -66,6 +66,11 @@ struct Rec24 {
 struct Rec4 {           // the records of oracle/ref_forms.cpp: id, then 32-bit keys a b c d
     std::uint64_t id;
     std::uint32_t a, b, c, d;
+    // the getters of oracle/ref_forms.cpp: by value, by reference, by pointer, by pointer chosen by an argument
+    std::uint32_t geta() const noexcept { return a; }
+    std::uint32_t const &refa() const noexcept { return a; }
+    std::uint32_t const *pointa() const noexcept { return &a; }
+    std::uint32_t const *pick(int k) const noexcept { return k ? &c : &a; }
 };
 
 static std::uint64_t splitmix(std::uint64_t &s) {
@@ -296,6 +301,43 @@ int main(int argc, char **argv) {
         showk("second level, isindexed2, index 2", kout);
         CHECK((rsbd8::radixsortcopy<A, N, 4, true>(n, kin, kout, 0, 1))); showk("second level, indirection2 4, isindexed2, index 1", kout);
         CHECK(rsbd8g_scratch_status(scratch, nullptr) == RSBD8G_OK);
+        {   // getters: the host evaluates them on managed copies of the records
+            Rec4 *mrec = nullptr;
+            cudaMallocManaged(reinterpret_cast<void **>(&mrec), n * sizeof(Rec4));
+            for (int i = 0; i < n; ++i) mrec[i] = h[i];
+            std::vector<Rec4 *> mp(n);
+            for (int i = 0; i < n; ++i) mp[i] = mrec + i;
+            Rec4 **min = todev(mp);
+            auto showm = [&](const char *t, Rec4 **d) {
+                auto o = tohost(d, n);
+                forms += t;
+                forms += ":";
+                for (auto p : o) forms += " " + std::to_string(p - mrec);
+                forms += "\n";
+            };
+            CHECK(rsbd8::radixsortcopy<&Rec4::geta>(n, min, dout)); showm("getter a", dout);
+            CHECK((rsbd8::radixsortcopy<&Rec4::geta, D>(n, min, dout))); showm("getter a desc", dout);
+            CHECK((rsbd8::radixsortcopy<&Rec4::refa, A, N, 4>(n, min, dout))); showm("getter reference a, indirection2 4", dout);
+            CHECK((rsbd8::radixsortcopy<&Rec4::pointa, A, N, 0, true>(n, min, dout, 0, 2)));
+            showm("getter pointer a, isindexed2, index 2", dout);
+            // the noalloc forms of getters: the keys go to the tail of the scratch
+            void *gscratch = nullptr;
+            cudaMalloc(&gscratch, rsbd8::gpuscratchbytesgetter<D, N, std::uint32_t>(n));
+            rsbd8::radixsortcopynoalloc<&Rec4::pointa, D, N, 4, true>(n, 0u, nullptr, gscratch, min, dout, dbuf, 2);
+            CHECK(rsbd8g_scratch_status(gscratch, nullptr) == RSBD8G_OK);
+            showm("getter pointer a desc, indirection2 4, isindexed2, index 2", dout);
+            {
+                Rec4 **mwork = todev(mp);
+                rsbd8::radixsortnoalloc<&Rec4::pick, A, N, 0, true>(n, 0u, nullptr, gscratch, mwork, dbuf, false, 1, 1);
+                CHECK(rsbd8g_scratch_status(gscratch, nullptr) == RSBD8G_OK);
+                showm("getter pick(1), isindexed2, index 1", mwork);
+                cudaFree(mwork);
+            }
+            CHECK((rsbd8::radixsortcopy<&Rec4::pick, A, N, 4>(n, min, dout, 0, 0))); showm("getter pick(0), indirection2 4", dout);
+            cudaFree(gscratch);
+            cudaFree(min);
+            cudaFree(mrec);
+        }
         std::fputs(forms.c_str(), stdout);
         if (!outdir.empty()) {
             FILE *f = std::fopen((outdir + "/forms.txt").c_str(), "w");

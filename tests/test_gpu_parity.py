@@ -492,3 +492,20 @@ def test_large_tile_pass_matches_oracle(dt, n, mode, direction):
     want = O.sortcopy(a, mode, direction, threads=8)
     assert same_bits(gpu_copy(a, mode, direction), want)
     assert same_bits(gpu_inplace(a, mode, direction), want)
+
+
+def test_loaded_module_is_sm103a():
+    """The CUDA runtime reports the library's kernels as compiled for sm_103a."""
+    assert R().api.binary_version() == 103
+
+
+@pytest.mark.parametrize("n", [12345, (1 << 23) + 17, (1 << 25) + 3])
+def test_crowded_digit_that_also_pads_the_last_tile(n):
+    """A descending sort whose fullest bucket (60 % of the keys: top byte 0) becomes ranked digit 255,
+    the digit the padding slots of a partial last tile take: the ballot-ranked digit and the padding
+    must rank exactly as the table would."""
+    a = S.uniform_bits(n % 991, n, np.uint32)
+    pick = (S.splitmix64(n, n) % np.uint64(10)) < np.uint64(6)
+    a[pick] &= np.uint32(0x00FFFFFF)
+    for d in ("dscfwdorder", "ascfwdorder"):
+        assert same_bits(gpu_copy(a, "native", d), O.sortcopy(a, "native", d, threads=8)), d

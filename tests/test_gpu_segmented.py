@@ -156,3 +156,66 @@ def test_segmented_pointer_tables_match_oracle(flags):
         del keep
         for x, o in zip(arrays, outs):
             assert same_bits(from_dev(o, np.uint32), O.sortcopy(x, "native", direction)), x.size
+
+
+@pytest.mark.parametrize("dt,mode", [(np.float32, "nativeabs"), (np.int32, "native"), (np.float64, "native"),
+                                     (np.uint16, "nativeabs")], ids=lambda x: str(getattr(x, "__name__", x)))
+def test_segmented_per_segment_directions_match_oracle(dt, mode):
+    """rsbd8g_segmented_sortcopy_ptrs_dirs: one launch sorts every array in its own direction --
+    small, cutoff-sized and multi-tile arrays, reverse tie order where the mode honours it."""
+    import torch
+    from radixsortbidi8_gb300 import api, batched as B
+    lens = [5, 0, 3000, 70001, 1, 40000, 9000, 250000, 33, 123457, 2, 16384]
+    dirs = [DIRS[i % 4] for i in range(len(lens))]
+    arrays = []
+    for i, n in enumerate(lens):
+        a, _ = _segments([n], dt, 300 + i)
+        arrays.append(a)
+    ins = [to_dev(a) if a.size else torch.empty(0, dtype=torch.int32, device="cuda") for a in arrays]
+    outs = [torch.empty_like(x) for x in ins]
+    bufs = [torch.empty_like(x) for x in ins]
+    total = sum(lens)
+    scratch = torch.empty(B.segmented_scratch_bytes(dt, total, len(lens), "ascfwdorder", mode), dtype=torch.uint8,
+                          device="cuda")
+    keep = B.segmented_sortcopy_ptrs(ins, outs, bufs, scratch, mode=mode, key_dtype=dt, directions=dirs)
+    assert api.scratch_status(scratch) == 0
+    del keep
+    for a, o, d in zip(arrays, outs, dirs):
+        if a.size:
+            assert same_bits(from_dev(o, dt), O.sortcopy(a, mode, d)), (a.size, d)
+
+
+def test_segmented_sixteen_byte_keys_match_oracle():
+    """128-bit integer keys (two 64-bit words each) in the contiguous segmented form: small,
+    cutoff-sized and multi-tile segments, every direction, against the oracle per segment; and the
+    serving loop on the same kind of keys."""
+    import torch
+    from radixsortbidi8_gb300 import batched as B, serving
+    lens = [0, 1, 2, 700, 1024, 1025, 5000, 3 * 3072 + 5, 70001, 12, 3072, 40000]
+    offs = np.zeros(len(lens) + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    n = int(offs[-1])
+    words = S.uniform_bits(61, 2 * n, np.uint64)
+    words[4::10] = words[0]
+    words[5::10] = words[1]                        # repeated keys
+    inp = torch.from_numpy(words.view(np.int64).copy()).cuda()
+    off_t = torch.from_numpy(offs).cuda()
+    for kind in ("u128", "i128"):
+        for d in DIRS:
+            s = B.SegmentedSorter(inp, off_t, d, "native", key_dtype=kind)
+            with torch.cuda.stream(s.stream):
+                s.run()
+            assert s.status() == 0
+            got = s.output.cpu().numpy().view(np.uint64)
+            for i in range(len(lens)):
+                seg = words[2 * offs[i]:2 * offs[i + 1]]
+                assert same_bits(got[2 * offs[i]:2 * offs[i + 1]], O.sortcopy_wide(seg, kind, "native", d)), (kind, d, i)
+    outs = [torch.empty(2 * m, dtype=torch.int64, device="cuda") for m in lens]
+    ins = [inp[2 * offs[i]:2 * offs[i + 1]] for i in range(len(lens))]
+    with serving.Server(budget_bytes=1 << 30, max_inflight=2) as srv:
+        ids = [srv.submit(ins[i], outs[i], DIRS[i % 4], "native", key_dtype="u128") for i in range(len(lens))]
+        srv.drain()
+        assert all(srv.wait(r).status == 0 for r in ids)
+    for i in range(len(lens)):
+        seg = words[2 * offs[i]:2 * offs[i + 1]]
+        assert same_bits(outs[i].cpu().numpy().view(np.uint64), O.sortcopy_wide(seg, "u128", "native", DIRS[i % 4])), i
