@@ -66,6 +66,9 @@ def parse_args():
     p.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
     p.add_argument("--rate", type=float, default=2000.0, help="serving: requests per second")
     p.add_argument("--batch-scale", type=float, default=1.0, help="batched: fraction of the segment counts")
+    p.add_argument("--calibrate-cpu", action="store_true",
+                   help="where the reference was compiled (oracle/_ref): time its sort beside the oracle's port "
+                        "on the same host cores and inputs, and print the ratio")
     return p.parse_args()
 
 
@@ -240,6 +243,9 @@ def gb300_arm(args, rank: int, world: int):
     for (out, buf, scr) in bufs:
         assert rs.scratch_status(scr, stream) == 0
 
+    # end to end first: large host-side work (the oracle's arrays) makes the next host<->device
+    # copies of pinned buffers slow for a while (measured: 12-25 GB/s against 190-210 GB/s)
+    e2e = None if args.no_e2e else e2e_arm(args, rs, arrays, stream)
     # correctness of the timed outputs: byte comparison with the oracle (the cpu_baseline leg's
     # checker, outside the timed region)
     check = "not checked (--no-cpu)" if args.no_cpu else verify_outputs(arrays, bufs)
@@ -288,7 +294,6 @@ def gb300_arm(args, rank: int, world: int):
 
     extra = uniform_u32(args, rs, dev, stream, peak)
     f32_rev = float32_abs_reverse(args, rs, arrays, stream)
-    e2e = None if args.no_e2e else e2e_arm(args, rs, arrays, stream)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(arrays, min(args.log2n, 24))
@@ -602,6 +607,50 @@ def reference_arm(args, rank: int, world: int) -> dict | None:
             "e2e": {"value": round(v, 4), "unit": "GKeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's CPU algorithm as the oracle's multithreaded C port (the reference's own "
                     "compiled code does not travel to this host)"}
+
+
+def calibrate_cpu(args) -> dict:
+    """The CPU baseline's calibration: the oracle's C port of the reference's LSD sort (what bench
+    times as the reference arm where the reference's own code cannot run) against the reference's own
+    rsbd8::radixsortcopy compiled from its header (oracle/_ref), on the same inputs and host cores.
+    float32 by absolute value has no reference timing (the reference's absolute modes write out of
+    bounds at this snapshot); the native-float descending sort of the same array stands in."""
+    import numpy as np
+    from oracle import oracle as O
+    from radixsortbidi8_gb300 import synth as S
+    if not O.ref_available():
+        return {"calibrate_cpu": "unavailable: oracle/_ref (the reference compiled from its header) is not built here"}
+    threads = os.cpu_count() or 1
+
+    def best(fn, reps=3):
+        t = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            t = min(t, time.perf_counter() - t0)
+        return t
+
+    rows = {}
+    for k in (24, 26):
+        n = 1 << k
+        cases = [("uint32_uniform", S.uniform_bits(SEEDS["u32"], n, np.uint32), "native", "ascfwdorder", True),
+                 ("uint32_low12", S.low_bits_u32(SEEDS["u32low12"], n), "native", "ascfwdorder", True),
+                 ("int64_uniform", S.uniform_bits(SEEDS["i64"], n, np.int64), "native", "ascfwdorder", True),
+                 ("float32_native_dscfwdorder", S.float_specials(SEEDS["f32"], n, np.float32), "native", "dscfwdorder", True),
+                 ("float32_abs_dscfwdorder", S.float_specials(SEEDS["f32"], n, np.float32), "nativeabs", "dscfwdorder", False)]
+        for name, a, m, d, ref_ok in cases:
+            O.sortcopy(a, m, d, threads=threads)                     # warm
+            tp = best(lambda: O.sortcopy(a, m, d, threads=threads))
+            row = {"port_gkeys_s": round(n / tp / 1e9, 4)}
+            if ref_ok:
+                O.ref_sortcopy(a, m, d)
+                tr = best(lambda: O.ref_sortcopy(a, m, d))
+                row["reference_gkeys_s"] = round(n / tr / 1e9, 4)
+                row["port_over_reference"] = round(tr / tp, 3)
+            rows[f"{name}_2p{k}"] = row
+    return {"calibrate_cpu": rows, "threads": threads, "host": os.uname().machine,
+            "note": "best of 3 after a warm-up; the reference with its default thread count "
+                    "(std::thread::hardware_concurrency), the port with the same number of threads"}
 
 
 def single_case(args) -> dict:
@@ -959,6 +1008,9 @@ def serving_config(args) -> dict:
 
 def main():
     args = parse_args()
+    if args.calibrate_cpu:
+        print(json.dumps(calibrate_cpu(args)), flush=True)
+        return
     if args.case:
         print(json.dumps(single_case(args)), flush=True)
         return

@@ -112,7 +112,14 @@ struct Batch {
     uint64_t keys = 0;
     double t_done = 0;
     bool launch_failed = false;
+    bool big = false;                  // one request that fills the GPU on its own
 };
+
+// Batch shapes.  A request of more than kAloneKeys keys fills the GPU by itself and runs as a batch
+// of its own; smaller requests are coalesced up to kBatchKeys keys, so a small request never waits
+// for a large one it was batched with.  Large batches leave one in-flight slot to small ones.
+constexpr uint64_t kAloneKeys = uint64_t(1) << 22;
+constexpr uint64_t kBatchKeys = uint64_t(1) << 24;
 
 // requests that one segmented launch can sort: the same key size, resolved filter (the kernels'
 // template mode) and flags; the direction is per segment (an unsigned key under "native" and under
@@ -144,7 +151,7 @@ struct Server {
 
     // statistics
     uint64_t completed = 0, keys_done = 0, batches = 0, max_coalesced = 0, max_inflight = 0;
-    uint64_t inflight = 0;
+    uint64_t inflight = 0, inflight_big = 0;
 
     ~Server() {
         {
@@ -202,6 +209,7 @@ struct Server {
             arena.release(b->tables_off, b->tables_bytes);
             slot_busy[size_t(b->slot)] = false;
             --inflight;
+            if (b->big) --inflight_big;
             delete b;
         }
         if (!done.empty()) cv.notify_all();
@@ -218,17 +226,30 @@ struct Server {
                     break;
                 }
             if (slot < 0) return nullptr;
-            // the head request decides the descriptor of this batch; take every pending request of
-            // that descriptor, in arrival order, while its buffer fits the budget
-            const Request *head = pending.front();
+            // the head: the oldest pending request that may start now (a large one only while a slot
+            // stays free for small requests).  It decides the group of the batch; a small head takes
+            // the pending small requests of its group, in arrival order, while the batch stays within
+            // kBatchKeys and their buffers fit the budget.
+            Request *head = nullptr;
+            const bool keep_slot = slot_busy.size() > 1 && inflight_big + 1 >= slot_busy.size();
+            for (Request *r : pending)
+                if (r->count <= kAloneKeys || !keep_slot) {
+                    head = r;
+                    break;
+                }
+            if (!head) return nullptr;
+            const bool big = head->count > kAloneKeys;
             const rsbd8g_desc key = head->desc;
             std::vector<Request *> take;
             uint64_t total = 0;
-            for (auto it = pending.begin(); it != pending.end() && take.size() < max_batch_requests;) {
-                Request *r = *it;
-                if (!same_group(*r, *head)) {
-                    ++it;
-                    continue;
+            for (Request *r : pending) {
+                if (take.size() >= max_batch_requests) break;
+                if (r != head) {
+                    if (big || take.empty()) {   // a large head runs alone; nothing goes before the head
+                        if (big && !take.empty()) break;
+                        continue;
+                    }
+                    if (!same_group(*r, *head) || r->count > kAloneKeys || total + r->count > kBatchKeys) continue;
                 }
                 size_t off;
                 r->buf_bytes = size_t(r->count) * key.key_bytes;
@@ -236,7 +257,6 @@ struct Server {
                 r->buf_off = off;
                 take.push_back(r);
                 total += r->count;
-                it = pending.erase(it);
             }
             if (take.empty()) return nullptr;    // memory is full: wait for a batch to finish
             size_t sb = 0;
@@ -251,21 +271,20 @@ struct Server {
                 ok = false;
             }
             if (!ok) {   // give the buffers back and retry when memory frees up
-                for (auto it = take.rbegin(); it != take.rend(); ++it) {
-                    arena.release((*it)->buf_off, (*it)->buf_bytes);
-                    pending.push_front(*it);
-                }
+                for (Request *r : take) arena.release(r->buf_off, r->buf_bytes);
                 if (inflight == 0) {   // nothing will free memory: fail the head request
-                    Request *r = pending.front();
-                    pending.pop_front();
-                    r->state = 2;
-                    r->status = RSBD8G_ERR_BUSY;
-                    r->t_done = now_s();
+                    pending.erase(std::find(pending.begin(), pending.end(), head));
+                    head->state = 2;
+                    head->status = RSBD8G_ERR_BUSY;
+                    head->t_done = now_s();
                     cv.notify_all();
                     continue;
                 }
                 return nullptr;
             }
+            for (Request *r : take) r->state = 1;
+            pending.erase(std::remove_if(pending.begin(), pending.end(), [](const Request *r) { return r->state == 1; }),
+                          pending.end());
             Batch *b = new Batch;
             b->srv = this;
             b->reqs = take;
@@ -277,6 +296,7 @@ struct Server {
             b->host_tables = slot_tables[size_t(slot)];
             b->host_err = slot_err[size_t(slot)];
             b->keys = total;
+            b->big = big;
             const double t = now_s();
             for (auto r : take) {
                 r->state = 1;
@@ -284,6 +304,7 @@ struct Server {
             }
             slot_busy[size_t(slot)] = true;
             ++inflight;
+            if (big) ++inflight_big;
             ++batches;
             max_coalesced = std::max<uint64_t>(max_coalesced, n);
             max_inflight = std::max(max_inflight, inflight);

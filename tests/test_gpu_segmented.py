@@ -209,7 +209,8 @@ def test_segmented_sixteen_byte_keys_match_oracle():
             got = s.output.cpu().numpy().view(np.uint64)
             for i in range(len(lens)):
                 seg = words[2 * offs[i]:2 * offs[i + 1]]
-                assert same_bits(got[2 * offs[i]:2 * offs[i + 1]], O.sortcopy_wide(seg, kind, "native", d)), (kind, d, i)
+                want = O.sortcopy_wide(seg, kind, "native", d).reshape(-1)
+                assert same_bits(got[2 * offs[i]:2 * offs[i + 1]], want), (kind, d, i)
     outs = [torch.empty(2 * m, dtype=torch.int64, device="cuda") for m in lens]
     ins = [inp[2 * offs[i]:2 * offs[i + 1]] for i in range(len(lens))]
     with serving.Server(budget_bytes=1 << 30, max_inflight=2) as srv:
@@ -218,4 +219,5 @@ def test_segmented_sixteen_byte_keys_match_oracle():
         assert all(srv.wait(r).status == 0 for r in ids)
     for i in range(len(lens)):
         seg = words[2 * offs[i]:2 * offs[i + 1]]
-        assert same_bits(outs[i].cpu().numpy().view(np.uint64), O.sortcopy_wide(seg, "u128", "native", DIRS[i % 4])), i
+        want = O.sortcopy_wide(seg, "u128", "native", DIRS[i % 4]).reshape(-1)
+        assert same_bits(outs[i].cpu().numpy().view(np.uint64), want), i
