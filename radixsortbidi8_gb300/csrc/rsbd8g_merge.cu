@@ -45,6 +45,7 @@ cudaError_t launch_merge2_t(const U *A, uint64_t na, const U *B, uint64_t nb, U 
     static int occ[64];
     std::call_once(once[dev & 63], [&] {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L::kBytes));
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kMergeThreads, L::kBytes);
         occ[dev & 63] = b > 0 ? b : 1;

@@ -40,23 +40,30 @@ __host__ __device__ __forceinline__ bool a_before_b(U a, U b, bool desc, bool a_
 // warp (all 32 lanes call it with the same arguments): each round probes 32 points of the interval
 // holding the answer and keeps the gap between the last true and the first false probe, so a
 // search over n elements takes about log32(n) dependent loads instead of log2(n)
-template <int MODE, typename U>
-__device__ __forceinline__ uint64_t merge_path_warp(const U *A, uint64_t na, const U *B, uint64_t nb, uint64_t d,
-                                                    bool desc, bool a_first) {
-    uint64_t lo = d > nb ? d - nb : 0, hi = d < na ? d : na;      // the answer lies in [lo, hi]
+// (`at_a(i)` / `at_b(j)`: element i of A, element j of B -- global arrays or the circular windows)
+template <int MODE, typename U, typename I, typename FA, typename FB>
+__device__ __forceinline__ I merge_path_warp_by(FA at_a, I na, FB at_b, I nb, I d, bool desc, bool a_first) {
+    I lo = d > nb ? d - nb : 0, hi = d < na ? d : na;             // the answer lies in [lo, hi]
     const uint32_t lane = threadIdx.x & 31u;
     while (hi - lo > 32) {
-        const uint64_t p = lo + (hi - lo) * (lane + 1) / 33;       // 32 increasing points of (lo, hi)
-        const bool t = a_before_b<MODE>(A[p], B[d - 1 - p], desc, a_first);
+        const I p = lo + I(uint64_t(hi - lo) * (lane + 1) / 33);   // 32 increasing points of (lo, hi)
+        const bool t = a_before_b<MODE>(at_a(p), at_b(d - 1 - p), desc, a_first);
         const int k = __popc(__ballot_sync(0xFFFFFFFFu, t));     // the true probes are a prefix
-        const uint64_t below = __shfl_sync(0xFFFFFFFFu, p, k > 0 ? k - 1 : 0);
-        const uint64_t above = __shfl_sync(0xFFFFFFFFu, p, k < 32 ? k : 31);
+        const I below = __shfl_sync(0xFFFFFFFFu, p, k > 0 ? k - 1 : 0);
+        const I above = __shfl_sync(0xFFFFFFFFu, p, k < 32 ? k : 31);
         if (k > 0) lo = below + 1;
         if (k < 32) hi = above;
     }
-    const uint64_t p = lo + lane;
-    const bool t = p < hi && a_before_b<MODE>(A[p], B[d - 1 - p], desc, a_first);
-    return lo + uint64_t(__popc(__ballot_sync(0xFFFFFFFFu, t)));
+    const I p = lo + lane;
+    const bool t = p < hi && a_before_b<MODE>(at_a(p), at_b(d - 1 - p), desc, a_first);
+    return lo + I(__popc(__ballot_sync(0xFFFFFFFFu, t)));
+}
+
+template <int MODE, typename U>
+__device__ __forceinline__ uint64_t merge_path_warp(const U *A, uint64_t na, const U *B, uint64_t nb, uint64_t d,
+                                                    bool desc, bool a_first) {
+    return merge_path_warp_by<MODE, U, uint64_t>([A](uint64_t i) { return A[i]; }, na,
+                                                 [B](uint64_t j) { return B[j]; }, nb, d, desc, a_first);
 }
 
 // the same search on the circular shared-memory windows of the persistent merge: element x of the
@@ -124,7 +131,13 @@ __global__ void __launch_bounds__(THREADS) k_merge2(const U *__restrict__ A, uin
     while (o < oend) {
         const uint32_t r = uint32_t(oend - o < uint64_t(TILE) ? oend - o : uint64_t(TILE));
         const uint32_t ca = uint32_t(aend - ia), cb = uint32_t(bend - ib);       // elements in the windows
-        if (tid == 0) misc[1] = merge_path_window<MODE, TILE>(wa, uint32_t(ia & M), ca, wb, uint32_t(ib & M), cb, r, dsc, af);
+        if (tid < 32) {      // the tile's share of A: one warp, 32 probes a round
+            const uint32_t a0 = uint32_t(ia & M), b0 = uint32_t(ib & M);
+            const uint32_t sp = merge_path_warp_by<MODE, U, uint32_t>([wa, a0](uint32_t i) { return wa[(a0 + i) & M]; }, ca,
+                                                                    [wb, b0](uint32_t j) { return wb[(b0 + j) & M]; }, cb,
+                                                                    r, dsc, af);
+            if (tid == 0) misc[1] = sp;
+        }
         __syncthreads();
         const uint32_t sa = uint32_t(misc[1]);
         const uint64_t ia2 = ia + sa, ib2 = ib + (r - sa);
@@ -144,13 +157,27 @@ __global__ void __launch_bounds__(THREADS) k_merge2(const U *__restrict__ A, uin
         if (d0 < r) {
             const uint32_t a0 = uint32_t(ia & M), b0 = uint32_t(ib & M);
             uint32_t xa = merge_path_window<MODE, TILE>(wa, a0, ca, wb, b0, cb, d0, dsc, af), xb = d0 - xa;
-            const uint32_t dend = d0 + ITEMS < r ? d0 + ITEMS : r;
-            for (uint32_t dd = d0; dd < dend; ++dd) {
-                bool take_a;
-                if (xa >= sa) take_a = false;                  // the tile's share of A is used up
-                else if (xb >= r - sa) take_a = true;
-                else take_a = a_before_b<MODE>(wa[(a0 + xa) & M], wb[(b0 + xb) & M], dsc, af);
-                sout[L::pad(dd)] = take_a ? wa[(a0 + xa++) & M] : wb[(b0 + xb++) & M];
+            const uint32_t cnt = r - d0 < uint32_t(ITEMS) ? r - d0 : uint32_t(ITEMS), nat = sa, nbt = r - sa;
+            // the next element of each side and its ordering key stay in registers: one load and one
+            // filter per output
+            U ua = wa[(a0 + xa) & M], ub = wb[(b0 + xb) & M];
+            U ka = order_key<MODE>(ua, dsc), kb = order_key<MODE>(ub, dsc);
+#pragma unroll
+            for (int q = 0; q < ITEMS; ++q) {
+                if (uint32_t(q) < cnt) {
+                    // A goes first unless its share of the tile is used up, B's is, or B orders first
+                    const bool take_a = xa < nat && (xb >= nbt || (af ? !key_less(kb, ka) : key_less(ka, kb)));
+                    sout[L::pad(d0 + q)] = take_a ? ua : ub;
+                    if (take_a) {
+                        ++xa;
+                        ua = wa[(a0 + xa) & M];
+                        ka = order_key<MODE>(ua, dsc);
+                    } else {
+                        ++xb;
+                        ub = wb[(b0 + xb) & M];
+                        kb = order_key<MODE>(ub, dsc);
+                    }
+                }
             }
         }
         __syncthreads();

@@ -111,8 +111,13 @@ def test_gpu_wide_argument_checks():
         rs.radixsortcopy(x[1:2001], y[1:2001], key_dtype="u128", count=1000)
     assert e.value.status == api.ERR_BAD_ARG
     offs = torch.tensor([0, 500, 1000], dtype=torch.int64, device="cuda")
-    with pytest.raises(api.RSBD8GError):                   # no segmented form for 16-byte keys
-        batched.segmented_scratch_bytes("u128", 1000, 2)
+    with pytest.raises(api.RSBD8GError):                   # x87 keys have no segmented form
+        batched.segmented_scratch_bytes("x87", 1000, 2)
+    nb = batched.segmented_scratch_bytes("u128", 1000, 2)  # 128-bit integers do
+    scr = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    with pytest.raises(api.RSBD8GError) as e:             # but their arrays must be 16-byte aligned
+        batched.segmented_sortcopy(x[1:2001], y[1:2001], torch.empty_like(y)[1:2001], offs, scr, key_dtype="u128")
+    assert e.value.status == api.ERR_BAD_ARG
 
 
 def test_gpu_wide_crowded_pass():
