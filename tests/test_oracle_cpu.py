@@ -264,3 +264,22 @@ def test_oracle_clean_under_address_and_undefined_behaviour_sanitizers(tmp_path)
     assert r.returncode == 0, r.stderr[-2000:]
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "PASS" in r.stdout, (r.stdout + r.stderr)[-4000:]
+
+
+def test_batched_oracle_equals_one_sort_per_array():
+    """rsbd8o_sortcopy_batch (segments of a batch, requests of a serving run: independent sorts
+    across threads) gives what one rsbd8o_sortcopy per array gives, empty and one-element arrays
+    included."""
+    from radixsortbidi8_gb300 import synth as S
+    lens = [0, 1, 2, 1000, 4097, 0, 30000, 3]
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    for dt, mode, d in ((np.uint32, "native", "ascfwdorder"), (np.float64, "nativeabs", "dscrevorder"),
+                        (np.int16, "nativetieredabs", "dscfwdorder")):
+        a = S.float_specials(3, int(offs[-1]), dt) if np.dtype(dt).kind == "f" else S.uniform_bits(3, int(offs[-1]), dt)
+        got = O.sortcopy_segments(a, offs, mode, d, threads=4)
+        for i in range(len(lens)):
+            want = O.sortcopy(a[offs[i]:offs[i + 1]], mode, d)
+            assert np.array_equal(got[offs[i]:offs[i + 1]].view(np.uint8), want.view(np.uint8)), (dt, i)
+        items = [(a[offs[i]:offs[i + 1]], mode, d) for i in range(len(lens))]
+        for g, (x, m, dd) in zip(O.sortcopy_batch(items, threads=3), items):
+            assert np.array_equal(g.view(np.uint8), O.sortcopy(x, m, dd).view(np.uint8))
