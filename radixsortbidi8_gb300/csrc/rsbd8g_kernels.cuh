@@ -605,6 +605,11 @@ __device__ __forceinline__ bool lookback_walk(const S *status, uint32_t tile, in
     return true;
 }
 
+// the signed offset from a staged slot to its output position: 32-bit while every count fits the
+// 30-bit look-back words (sorts of fewer than 2^30 keys), 64-bit beyond
+template <typename S>
+using TileOffset = std::conditional_t<std::is_same_v<S, uint32_t>, int32_t, long long>;
+
 template <typename U, bool HAS_VAL, int THREADS>
 constexpr int onesweep_min_blocks() {
     return THREADS >= 512 ? 2 : (HAS_VAL ? 3 : (sizeof(U) <= 4 ? 4 : 3));
@@ -637,7 +642,8 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
     U *stage_k = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *wofs = reinterpret_cast<uint32_t *>(smem + L::kOffWofs);
-    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    using G = TileOffset<S>;
+    G *gofs = reinterpret_cast<G *>(smem + L::kOffGofs);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);  // [1] bad [2..9] scan
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t *urow = R::row(wofs);
@@ -693,7 +699,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
                            StatusWord<S>::make(kStInclusive, excl + count));
         }
         if (bad) misc[1] = 1u;
-        gofs[tid] = (long long)(bstart[tid] + excl) - (long long)ts;
+        gofs[tid] = G((long long)(bstart[tid] + excl) - (long long)ts);
     }
     __syncthreads();
     const bool tile_bad = misc[1] != 0 || tile == stall_tile;
@@ -715,7 +721,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
             for (int i = 0; i < ITEMS; ++i) {
                 const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
                 const U k = stage_k[s];
-                const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                const G g = gofs[pass_digit<MODE>(k, pass, dmask)] + G(s);
                 if (uint64_t(g) < n) {
                     if (t.dst_k) t.dst_k[g] = k;
                     if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
@@ -726,7 +732,7 @@ __device__ __forceinline__ void sweep_tile(unsigned char *smem, const SweepTile<
         } else {
             for (uint32_t s = tid; s < tvalid; s += THREADS) {
                 const U k = stage_k[s];
-                const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                const G g = gofs[pass_digit<MODE>(k, pass, dmask)] + G(s);
                 if (uint64_t(g) < n) {
                     if (t.dst_k) t.dst_k[g] = k;
                     if constexpr (HAS_VAL) t.dst_v[g] = stage_v[s];
@@ -845,7 +851,8 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
     U *stage = reinterpret_cast<U *>(smem);
     uint64_t *stage_v = reinterpret_cast<uint64_t *>(smem + L::kOffV);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
-    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    using G = TileOffset<S>;
+    G *gofs = reinterpret_cast<G *>(smem + L::kOffGofs);
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
     uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
     uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
@@ -953,7 +960,7 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
                     st_relaxed(status + size_t(tileA) * kBuckets + d, StatusWord<S>::make(kStInclusive, excl + count));
             }
             if (bad) misc[1] = 1u;
-            gofs[d] = (long long)(bstart[d] + excl) - (long long)tsA[d];
+            gofs[d] = G((long long)(bstart[d] + excl) - (long long)tsA[d]);
         }
         __syncthreads();                                                        // barrier 2
 
@@ -984,7 +991,7 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
                 for (int i = 0; i < ITEMS; ++i) {
                     const uint32_t s = uint32_t(tid) + uint32_t(i) * THREADS;
                     const U k = stage[s];
-                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    const G g = gofs[pass_digit<MODE>(k, pass, dmask)] + G(s);
                     if (uint64_t(g) < n) {
                         if (!HAS_VAL || dst) dst[g] = k;
                         if constexpr (HAS_VAL) dst_v[g] = stage_v[s];
@@ -995,7 +1002,7 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
             } else {
                 for (uint32_t s = tid; s < tvalidA; s += THREADS) {
                     const U k = stage[s];
-                    const long long g = gofs[pass_digit<MODE>(k, pass, dmask)] + (long long)s;
+                    const G g = gofs[pass_digit<MODE>(k, pass, dmask)] + G(s);
                     if (uint64_t(g) < n) {
                         if (!HAS_VAL || dst) dst[g] = k;
                         if constexpr (HAS_VAL) dst_v[g] = stage_v[s];

@@ -30,8 +30,11 @@ namespace rsbd8g {
 namespace {
 
 constexpr int kMergeThreads = 256;
+// outputs per thread and tile: 4096-key tiles up to 4-byte keys; 2048 for 8-byte keys (four CTAs of
+// 49 KB per SM instead of two of 97 KB: 2^28 int64 merge 1.51 -> 1.34 ms; 4-byte keys were slower
+// with 2048-key tiles, 0.82 -> 0.93 ms) and 1024 for 16-byte keys
 template <typename U>
-constexpr int merge_items() { return sizeof(U) >= 16 ? 8 : 16; }
+constexpr int merge_items() { return sizeof(U) >= 16 ? 4 : (sizeof(U) == 8 ? 8 : 16); }
 
 template <typename U, int MODE>
 cudaError_t launch_merge2_t(const U *A, uint64_t na, const U *B, uint64_t nb, U *out, bool desc, bool a_first,

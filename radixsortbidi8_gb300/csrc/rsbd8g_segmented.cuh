@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
-    long long *gofs = reinterpret_cast<long long *>(smem + L::kOffGofs);
+    int32_t *gofs = reinterpret_cast<int32_t *>(smem + L::kOffGofs);   // segments hold fewer than 2^30 keys
     uint32_t *tsall = reinterpret_cast<uint32_t *>(smem + L::kOffTs);
     uint32_t *cntall = reinterpret_cast<uint32_t *>(smem + L::kOffCnt);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);   // [0] next tile [1] bad [2..9] scan
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(THREADS, 2)
                                StatusWord<uint32_t>::make(kStInclusive, excl + count));
             }
             if (bad) misc[1] = 1u;
-            gofs[d] = (long long)(uint64_t(A.bs[d]) + excl) - (long long)tsA[d];
+            gofs[d] = int32_t((long long)(uint64_t(A.bs[d]) + excl) - (long long)tsA[d]);
         }
         __syncthreads();                                                        // barrier 2
 
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(THREADS, 2)
             const uint64_t n = A.n;
             for (uint32_t s = tid; s < tvalidA; s += THREADS) {
                 const U k = stage[s];
-                const long long g = gofs[pass_digit<MODE>(k, pass, A.dmask)] + (long long)s;
+                const int32_t g = gofs[pass_digit<MODE>(k, pass, A.dmask)] + int32_t(s);
                 if (uint64_t(g) < n) dst[g] = k;
                 else atomicOr(err_word, kDevFault);     // an offset outside the segment: flagged, not written
             }

@@ -150,3 +150,17 @@ def test_chunked_sort_refuses_a_budget_too_small_for_two_keys():
     with pytest.raises(api.RSBD8GError) as e:
         api.radixsortcopy_chunked(a, out, key_dtype=np.uint32, device_bytes=1024)
     assert e.value.status == api.ERR_TOO_LARGE
+
+
+def test_chunked_sort_of_sixteen_byte_keys():
+    """128-bit integer keys in host memory, sorted in chunks within a small device budget."""
+    from radixsortbidi8_gb300 import api
+    n = 200003
+    words = S.uniform_bits(17, 2 * n, np.uint64)
+    words[6::14] = words[0]
+    words[7::14] = words[1]
+    out = np.empty_like(words)
+    for d in ("ascfwdorder", "dscfwdorder"):
+        assert api.radixsortcopy_chunked(words, out, d, "native", key_dtype="i128", device_bytes=2 << 20)
+        want = O.sortcopy_wide(words, "i128", "native", d).reshape(-1)
+        assert same_bits(out, want), d
