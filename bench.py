@@ -355,6 +355,8 @@ def uniform_u32(args, rs, dev, stream, peak) -> dict:
     bits = S.uniform_bits_torch(SEEDS["u32"], n, 4, device=dev)
     out, buf = torch.empty_like(bits), torch.empty_like(bits)
     scr = torch.empty(rs.scratch_bytes(np.uint32, n), dtype=torch.uint8, device=dev)
+    # the input was made, and these arrays allocated, on the default stream; the sorts run on `stream`
+    torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         for _ in range(max(3, args.warmup)):
             rs.radixsortcopynoalloc(bits, out, buf, scr, key_dtype=np.uint32, stream=stream)
@@ -394,6 +396,7 @@ def float32_abs_reverse(args, rs, arrays, stream) -> dict:
                       device=bits.device)
     run = lambda: rs.radixsortcopynoalloc(bits, out, buf, scr, "dscrevorder", "nativeabs", key_dtype=np.float32,
                                           stream=stream)
+    torch.cuda.synchronize()                  # allocated on the default stream, used on `stream`
     for _ in range(max(3, args.warmup)):
         run()
     torch.cuda.synchronize()
@@ -438,6 +441,7 @@ def e2e_arm(args, rs, arrays, stream) -> dict:
                     for _, b, kdt, d, m in arrays],
             "host_out": [torch.empty_like(h).pin_memory() for h in host_in],
         })
+    torch.cuda.synchronize()                  # the buffers are used on the stage streams below
     # pipeline: one stream per stage; events order each array's H2D -> sort -> D2H and keep a
     # buffer set from being refilled before the step two back has finished with it
     s_h2d, s_sort, s_d2h = (torch.cuda.Stream(device=dev) for _ in range(3))
@@ -746,6 +750,7 @@ def config1_small(args, rs, dev, stream) -> dict:
     out, buf = torch.empty_like(bits), torch.empty_like(bits)
     scr = torch.empty(rs.scratch_bytes(np.uint32, n), dtype=torch.uint8, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()                  # made on the default stream, used on `stream`
     times = []
     with torch.cuda.stream(stream):
         for i in range(max(3, args.warmup) + max(10, args.steps)):
@@ -781,6 +786,7 @@ def config3_records(args, rs, dev, stream, peak) -> dict:
     scr = torch.empty(rs.scratch_bytes(np.float64, n, indirection=api.MEMBER, offset1=8), dtype=torch.uint8,
                       device=dev)
     run = lambda: rs.radixsortcopynoalloc_member(ptrs, out, buf, scr, np.float64, 8, stream=stream)
+    torch.cuda.synchronize()                  # records and pointers made on the default stream
     with torch.cuda.stream(stream):
         for _ in range(max(3, args.warmup)):
             run()
@@ -824,6 +830,7 @@ def batched_run(args, which: str, steps: int, check: bool) -> dict:
     kdt = np.uint32 if which.startswith("A") else np.float64
     keys = S.batch_keys_torch(which, total, device=dev)
     off_t = torch.from_numpy(offs).to(dev)
+    torch.cuda.synchronize()
     sorter = B.SegmentedSorter(keys, off_t, key_dtype=kdt).capture()
     for _ in range(max(1, args.warmup)):
         sorter.replay()
@@ -896,6 +903,7 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     ring_pos = [0, 0, 0, 0]
     ring_owner = [[], [], [], []]           # (start, end, request id) still possibly in flight
     starts = (S.splitmix64(S.SERVING_SEED, nreq, stream=44) % np.uint64(pool_n - (1 << 26))).astype(np.int64)
+    torch.cuda.synchronize()                  # the pools are read, and the rings written, on the server's streams
     srv = serving.Server(budget_bytes=64 << 30, max_inflight=4)
     ids, metas = [], []
 
@@ -961,6 +969,7 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     # closed loop: a prefix of the same requests, queued at once vs a plain allocating-sort loop
     m_req = min(nreq, closed)
     outs = [torch.empty(int(lens[i]), dtype=kinds[kind[i]][1], device=dev) for i in range(m_req)]
+    torch.cuda.synchronize()
     srv2 = serving.Server(budget_bytes=64 << 30, max_inflight=4)
     for i in range(min(m_req, 64)):          # warm-up of kernels and module loading
         d, m = dm(i)

@@ -274,10 +274,13 @@ RSBD8G_API rsbd8g_status rsbd8g_segmented_sortcopy_ptrs_dirs(const rsbd8g_desc *
  * of it) and starts a dispatcher thread.  rsbd8g_server_submit queues one request (device input
  * and output arrays of `count` keys, direct keys only, < 2^30 keys) from any host thread and
  * returns at once; the dispatcher admits pending requests in arrival order while the budget and
- * the `max_inflight` batch slots allow, coalesces the admitted requests that share a descriptor
- * into one batched launch on its own stream, and retires batches as they finish, so requests
- * arriving while others run are admitted and overlap on the device.  A request that can never
- * fit the budget is refused (RSBD8G_ERR_BUSY).  Times are seconds on a steady host clock.
+ * the `max_inflight` batch slots allow, coalesces admitted requests of the same key type, mode and
+ * flags (directions may differ) into one batched launch on its own stream, and retires batches as
+ * they finish, so requests arriving while others run are admitted and overlap on the device.  The
+ * server's streams are not ordered after any stream of the caller: the input must already hold
+ * its keys when it is submitted (the work that wrote it has finished), and neither array may be
+ * used by other work until the request is done.  A request that can never fit the budget is
+ * refused (RSBD8G_ERR_BUSY).  Times are seconds on a steady host clock.
  * No counterpart in the reference. */
 typedef struct rsbd8g_server rsbd8g_server;
 

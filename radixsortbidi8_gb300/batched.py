@@ -121,7 +121,11 @@ def segmented_sortcopy(input, output, buffer, offsets, scratch, direction="ascfw
 
 class SegmentedSorter:
     """Buffers for one batch shape; ``run`` sorts, ``capture`` records one CUDA graph of the call
-    and ``replay`` launches it (one graph launch per batch)."""
+    and ``replay`` launches it (one graph launch per batch).
+
+    The sort runs on the sorter's own stream, ordered after the work already queued on the
+    caller's current stream (which made the input and allocated the buffers) and before the work
+    the caller queues after the call, as a call on the current stream would be."""
 
     def __init__(self, input, offsets, direction="ascfwdorder", mode="native", key_dtype=None,
                  tuning: SegTuning | None = None, stream=None):
@@ -139,25 +143,47 @@ class SegmentedSorter:
         self.stream = stream if stream is not None else torch.cuda.Stream(device=input.device)
         self.graph = None
 
-    def run(self):
+    def _after_caller(self):
+        """the sorter's stream waits for the caller's queued work; returns the caller's stream"""
+        import torch
+        cur = torch.cuda.current_stream(self.input.device)
+        if cur != self.stream:
+            self.stream.wait_stream(cur)
+        return cur
+
+    def _before_caller(self, cur) -> None:
+        """the caller's later work waits for the sort"""
+        if cur != self.stream:
+            cur.wait_stream(self.stream)
+
+    def _sort(self):
         segmented_sortcopy(self.input, self.output, self.buffer, self.offsets, self.scratch, self.direction,
                            self.mode, self.key_dtype, self.tuning, self.stream)
+
+    def run(self):
+        cur = self._after_caller()
+        self._sort()
+        self._before_caller(cur)
         return self.output
 
     def capture(self):
         import torch
+        cur = self._after_caller()
         with torch.cuda.stream(self.stream):
-            self.run()                 # first call outside capture: kernel attributes, module loading
+            self._sort()               # first call outside capture: kernel attributes, module loading
             self.stream.synchronize()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph, stream=self.stream):
-                self.run()
+                self._sort()
+        self._before_caller(cur)
         return self
 
     def replay(self):
         import torch
+        cur = self._after_caller()
         with torch.cuda.stream(self.stream):       # a graph launches on the current stream
             self.graph.replay()
+        self._before_caller(cur)
         return self.output
 
     def status(self) -> int:
@@ -178,6 +204,11 @@ def sort_each(input, output, offsets_host: np.ndarray, direction="ascfwdorder", 
     ip, op, bp = input.data_ptr(), output.data_ptr(), buf.data_ptr()
     L = api.lib()
     d = api.make_desc(kd, direction, mode)
+    cur = torch.cuda.current_stream(input.device)
+    if isinstance(stream, torch.cuda.Stream) and stream != cur:
+        stream.wait_stream(cur)                 # the buffers above were allocated on the caller's stream
+    elif stream is not None and not isinstance(stream, torch.cuda.Stream):
+        cur.synchronize()                       # a raw stream handle: wait on the host instead
     st = api._stream(stream)
     nb = scratch.numel()
     sp = scratch.data_ptr()
@@ -219,6 +250,7 @@ def autotune(key_bytes_list=(2, 4, 8), nsegs: int = 20000, lo: int = 16, hi: int
             for cutoff in sorted({cap // 4, cap // 2, cap}):
                 t = SegTuning(v, cutoff)
                 s = SegmentedSorter(keys, offs, key_dtype=kd[kb], tuning=t)
+                torch.cuda.current_stream().synchronize()    # keys made, buffers allocated on this stream
                 with torch.cuda.stream(s.stream):
                     s.run()
                     s.stream.synchronize()

@@ -37,11 +37,38 @@ struct Filter {
     uint32_t absv, sign, fltp, desc;
 };
 
+// The arrays of one sort reach the scatter and copy kernels as a kernel parameter; the plan in
+// the control block (scratch memory, which the caller owns) names them by index.  So no address
+// is ever read from scratch: a control block damaged by a caller's stray write gives wrong
+// results and a fault flag, never an access outside the sort's own arrays.
+enum : uint32_t { kArrIn = 0u, kArrOut = 1u, kArrBuf = 2u, kArrKeysA = 3u, kArrKeysB = 4u, kArrCount = 5u,
+                  kArrNone = 0xFFu };
+struct SortArrays {
+    const void *p[kArrCount];   // input, output, buffer, indirect key arrays A and B (null if unused)
+};
+// array `sel`; null for kArrNone; `fallback` (with *bad set) for an index that names no array.
+// Selects over constant indices, so the parameter array is never indexed at run time (which
+// would copy it to local memory).
+__host__ __device__ __forceinline__ void *sort_array(const SortArrays &a, uint32_t sel, uint32_t fallback, bool *bad) {
+    if (sel == kArrNone) return nullptr;
+    const void *r = nullptr, *f = nullptr;
+#pragma unroll
+    for (uint32_t i = 0; i < kArrCount; ++i) {
+        r = sel == i ? a.p[i] : r;
+        f = fallback == i ? a.p[i] : f;
+    }
+    if (!r) {
+        *bad = true;
+        r = f;
+    }
+    return const_cast<void *>(r);
+}
+
 struct PassPlan {
-    const void *src_keys;
-    void *dst_keys;        // may be null on the last indirect pass (keys are dropped)
-    const void *src_vals;  // indirect: object pointers
-    void *dst_vals;
+    uint32_t src_keys;     // SortArrays indices
+    uint32_t dst_keys;     // kArrNone on the last indirect pass (keys are dropped)
+    uint32_t src_vals;     // indirect: object pointers (kArrNone for direct sorts)
+    uint32_t dst_vals;
     uint32_t active;
     uint32_t reverse;      // read the source back to front (isrevorder, first surviving pass)
     uint32_t hot;          // crowded digits of the pass, ranked with ballots: (digit1 << 16) | digit0,
@@ -57,9 +84,8 @@ struct Control {
     uint32_t tile_counter[kMaxPasses];
     uint32_t active_passes;
     uint32_t copy_mode;
-    const void *copy_src;
-    void *copy_dst;
-    uint64_t copy_elem_bytes;
+    uint32_t copy_src;     // SortArrays indices
+    uint32_t copy_dst;
     uint32_t stall_tile;   // diagnostics: this tile never publishes (0xFFFFFFFF = off)
     uint32_t prefetch;     // 1: every array is device memory, so tiles may be prefetched into L2
     uint64_t spin_limit_ns;

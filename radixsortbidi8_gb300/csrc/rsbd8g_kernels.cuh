@@ -177,12 +177,6 @@ __global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__
 // ---- scan, pass-skip and plan -----------------------------------------------------------------
 
 struct PlanArgs {
-    const void *in;
-    void *out;
-    void *buf;
-    void *keys_a;
-    void *keys_b;
-    uint64_t elem_bytes;   // bytes moved per element in the copy step (key bytes, or 8 for pointers)
     uint64_t spin_limit_ns;
     uint32_t inplace;      // radixsort / radixsortnoalloc: sort `in` using `buf`
     uint32_t to_buffer;    // movetobuffer
@@ -256,9 +250,8 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
     ctrl->stall_tile = a.stall_tile;
     ctrl->prefetch = a.prefetch;
     ctrl->copy_mode = kCopyNone;
-    ctrl->copy_elem_bytes = a.elem_bytes;
-    const void *cur = a.in;               // where the data (values for indirection) is
-    const void *curk = a.keys_a;          // indirection: where the filtered keys are
+    uint32_t cur = kArrIn;                // where the data (values for indirection) is
+    uint32_t curk = kArrKeysA;            // indirection: where the filtered keys are
     int i = 0;
     for (int p = 0; p < int(a.passes); ++p) {
         PassPlan &pp = ctrl->plan[p];
@@ -266,41 +259,41 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
         pp.hot = hot[p];
         if (skip[p]) continue;
         ++i;
-        void *dst;
-        if (a.inplace) dst = (cur == a.in) ? a.buf : const_cast<void *>(a.in);
-        else dst = ((k - i) % 2 == 0) ? a.out : a.buf;
+        uint32_t dst;
+        if (a.inplace) dst = (cur == kArrIn) ? kArrBuf : kArrIn;
+        else dst = ((k - i) % 2 == 0) ? kArrOut : kArrBuf;
         pp.reverse = (i == 1) && a.rev;
         if (a.indirect) {
             pp.src_vals = cur;
             pp.dst_vals = dst;
             pp.src_keys = curk;
-            void *dk = (curk == a.keys_a) ? a.keys_b : a.keys_a;
-            pp.dst_keys = (i == k) ? nullptr : dk;
+            const uint32_t dk = (curk == kArrKeysA) ? kArrKeysB : kArrKeysA;
+            pp.dst_keys = (i == k) ? kArrNone : dk;
             curk = dk;
         } else {
             pp.src_keys = cur;
             pp.dst_keys = dst;
-            pp.src_vals = nullptr;
-            pp.dst_vals = nullptr;
+            pp.src_vals = kArrNone;
+            pp.dst_vals = kArrNone;
         }
         cur = dst;
     }
     if (!a.inplace) {
         if (k == 0) {
             ctrl->copy_mode = a.rev ? kCopyReversed : kCopyPlain;
-            ctrl->copy_src = a.in;
-            ctrl->copy_dst = a.out;
+            ctrl->copy_src = kArrIn;
+            ctrl->copy_dst = kArrOut;
         }
     } else {
-        const void *target = a.to_buffer ? a.buf : a.in;
+        const uint32_t target = a.to_buffer ? kArrBuf : kArrIn;
         if (k == 0 && a.rev) {
             ctrl->copy_mode = a.to_buffer ? kCopyReversed : kReverseInPlace;
-            ctrl->copy_src = a.in;
-            ctrl->copy_dst = const_cast<void *>(target);
+            ctrl->copy_src = kArrIn;
+            ctrl->copy_dst = target;
         } else if (cur != target) {
             ctrl->copy_mode = kCopyPlain;
             ctrl->copy_src = cur;
-            ctrl->copy_dst = const_cast<void *>(target);
+            ctrl->copy_dst = target;
         }
     }
 }
@@ -754,17 +747,23 @@ __device__ __forceinline__ void sweep_init_smem(unsigned char *smem) {
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S, int HOT>
 __device__ __forceinline__ void onesweep_body(unsigned char *smem, Control *__restrict__ ctrl,
-                                              const PassPlan &plan, const unsigned long long *__restrict__ bstart_all,
+                                              const PassPlan &plan, const SortArrays &arrs,
+                                              const unsigned long long *__restrict__ bstart_all,
                                               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles,
                                               uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     unsigned long long *bstart = reinterpret_cast<unsigned long long *>(smem + L::kOffBstart);
     uint32_t *misc = reinterpret_cast<uint32_t *>(smem + L::kOffMisc);
     SweepTile<U, S> t;
-    t.src_k = static_cast<const U *>(plan.src_keys);
-    t.dst_k = static_cast<U *>(plan.dst_keys);
-    t.src_v = static_cast<const uint64_t *>(plan.src_vals);
-    t.dst_v = static_cast<uint64_t *>(plan.dst_vals);
+    bool bad = false;
+    t.src_k = static_cast<const U *>(sort_array(arrs, plan.src_keys, HAS_VAL ? kArrKeysA : kArrIn, &bad));
+    t.dst_k = static_cast<U *>(sort_array(arrs, plan.dst_keys, HAS_VAL ? kArrKeysB : kArrBuf, &bad));
+    t.src_v = static_cast<const uint64_t *>(sort_array(arrs, plan.src_vals, kArrIn, &bad));
+    t.dst_v = static_cast<uint64_t *>(sort_array(arrs, plan.dst_vals, kArrBuf, &bad));
+    if (bad || !t.src_k || (HAS_VAL ? (!t.src_v || !t.dst_v) : !t.dst_k)) {   // a damaged control block
+        if (threadIdx.x == 0) atomicOr(&ctrl->error, kDevFault);
+        return;
+    }
     t.status = status;
     t.n = n;
     t.reverse = plan.reverse != 0;
@@ -797,7 +796,7 @@ __device__ __forceinline__ void onesweep_body(unsigned char *smem, Control *__re
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
-    k_onesweep(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
+    k_onesweep(Control *__restrict__ ctrl, const SortArrays arrs, const unsigned long long *__restrict__ bstart_all,
                S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
@@ -807,9 +806,11 @@ __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREA
     if (!plan.active) return;
     // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
     if (plan.hot == kNoHotPair)
-        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, bstart_all, status, pass, n, num_tiles, dmask);
+        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, arrs, bstart_all, status, pass, n, num_tiles,
+                                                              dmask);
     else
-        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, bstart_all, status, pass, n, num_tiles, dmask);
+        onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, arrs, bstart_all, status, pass, n, num_tiles,
+                                                              dmask);
 }
 
 // ---- the pipelined scatter pass -----------------------------------------------------------------
@@ -841,6 +842,7 @@ struct PipeSmem {
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S, int HOT>
 __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control *__restrict__ ctrl, const PassPlan &plan,
+                                                   const SortArrays &arrs,
                                                    const unsigned long long *__restrict__ bstart_all,
                                                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles,
                                                    uint32_t dmask) {
@@ -862,10 +864,16 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
     constexpr bool kSplit = R::kUnits == 32;
     uint32_t *half = reinterpret_cast<uint32_t *>(smem + L::kOffHalf);
 
-    const U *src = static_cast<const U *>(plan.src_keys);
-    U *dst = static_cast<U *>(plan.dst_keys);       // null: keys are dropped (last pass of an indirect sort)
-    const uint64_t *src_v = static_cast<const uint64_t *>(plan.src_vals);
-    uint64_t *dst_v = static_cast<uint64_t *>(plan.dst_vals);
+    bool bad_plan = false;
+    const U *src = static_cast<const U *>(sort_array(arrs, plan.src_keys, HAS_VAL ? kArrKeysA : kArrIn, &bad_plan));
+    U *dst = static_cast<U *>(sort_array(arrs, plan.dst_keys, HAS_VAL ? kArrKeysB : kArrBuf, &bad_plan));  // null: keys
+                                                                       // are dropped (last pass of an indirect sort)
+    const uint64_t *src_v = static_cast<const uint64_t *>(sort_array(arrs, plan.src_vals, kArrIn, &bad_plan));
+    uint64_t *dst_v = static_cast<uint64_t *>(sort_array(arrs, plan.dst_vals, kArrBuf, &bad_plan));
+    if (bad_plan || !src || (HAS_VAL ? (!src_v || !dst_v) : !dst)) {   // a damaged control block
+        if (threadIdx.x == 0) atomicOr(&ctrl->error, kDevFault);
+        return;
+    }
     const bool reverse = plan.reverse != 0;
     const uint64_t spin_limit = ctrl->spin_limit_ns;
     const uint32_t stall_tile = ctrl->stall_tile;
@@ -1040,7 +1048,7 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, 2)
-    k_onesweep_pipe(Control *__restrict__ ctrl, const unsigned long long *__restrict__ bstart_all,
+    k_onesweep_pipe(Control *__restrict__ ctrl, const SortArrays arrs, const unsigned long long *__restrict__ bstart_all,
                     S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
     static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
     static_assert(PipeSmem<U, THREADS, ITEMS, HAS_VAL>::kTile <= 65535, "tile ranks are 16-bit");
@@ -1049,10 +1057,10 @@ __global__ void __launch_bounds__(THREADS, 2)
     if (!plan.active) return;
     // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
     if (plan.hot == kNoHotPair)
-        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, bstart_all, status, pass, n,
+        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, arrs, bstart_all, status, pass, n,
                                                                    num_tiles, dmask);
     else
-        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, bstart_all, status, pass, n,
+        onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 1>(smem, ctrl, plan, arrs, bstart_all, status, pass, n,
                                                                    num_tiles, dmask);
 }
 
@@ -1060,9 +1068,7 @@ __global__ void __launch_bounds__(THREADS, 2)
 // ---- copy step --------------------------------------------------------------------------------
 
 template <typename T>
-__device__ __forceinline__ void copy_elems(const Control &c, uint64_t n) {
-    const T *src = static_cast<const T *>(c.copy_src);
-    T *dst = static_cast<T *>(c.copy_dst);
+__device__ __forceinline__ void copy_elems(const Control &c, const T *src, T *dst, uint64_t n) {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     const uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c.copy_mode == kCopyPlain) {
@@ -1078,15 +1084,26 @@ __device__ __forceinline__ void copy_elems(const Control &c, uint64_t n) {
     }
 }
 
-static __global__ void __launch_bounds__(256) k_copy(const Control *__restrict__ ctrl, uint64_t n) {
+// the copy step; elem_bytes (a kernel parameter, like the arrays) is the size of one element
+static __global__ void __launch_bounds__(256) k_copy(Control *__restrict__ ctrl, const SortArrays arrs, uint64_t n,
+                                                     uint32_t elem_bytes) {
     const Control c = *ctrl;
     if (c.copy_mode == kCopyNone) return;
-    switch (c.copy_elem_bytes) {
-        case 1: copy_elems<uint8_t>(c, n); break;
-        case 2: copy_elems<uint16_t>(c, n); break;
-        case 4: copy_elems<uint32_t>(c, n); break;
-        case 8: copy_elems<uint64_t>(c, n); break;
-        default: copy_elems<uint4>(c, n); break;          // 16-byte elements
+    bool bad = false;
+    const void *src = sort_array(arrs, c.copy_src, kArrIn, &bad);
+    void *dst = sort_array(arrs, c.copy_dst, kArrBuf, &bad);
+    if (bad || !src || !dst) {      // a damaged control block
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctrl->error, kDevFault);
+        return;
+    }
+    switch (elem_bytes) {
+        case 1: copy_elems<uint8_t>(c, static_cast<const uint8_t *>(src), static_cast<uint8_t *>(dst), n); break;
+        case 2: copy_elems<uint16_t>(c, static_cast<const uint16_t *>(src), static_cast<uint16_t *>(dst), n); break;
+        case 4: copy_elems<uint32_t>(c, static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst), n); break;
+        case 8: copy_elems<uint64_t>(c, static_cast<const uint64_t *>(src), static_cast<uint64_t *>(dst), n); break;
+        default:                   // 16-byte elements
+            copy_elems<uint4>(c, static_cast<const uint4 *>(src), static_cast<uint4 *>(dst), n);
+            break;
     }
 }
 

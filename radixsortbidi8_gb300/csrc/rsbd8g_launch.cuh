@@ -18,8 +18,8 @@ constexpr int kHistThreads = 512;         // gather histogram (indirect keys)
 constexpr int kHistDirectThreads = 1024;  // direct keys: one CTA per SM
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
-cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch, uint32_t dmask,
-                            cudaStream_t s) {
+cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch,
+                            const SortArrays &arrs, uint32_t dmask, cudaStream_t s) {
     // the pipelined pass, unless there are too few tiles to fill its pipeline (a sort of about one
     // tile per CTA runs each tile's phases back to back in k_onesweep instead)
     using SM = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
@@ -51,9 +51,9 @@ cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsign
         S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
         LaunchTimer t(s, RSBD8G_KERNEL_ONESWEEP, uint32_t(sizeof(U)), p, n);
         if (pipe)
-            pkern<<<grid, THREADS, PM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
+            pkern<<<grid, THREADS, PM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask);
         else
-            kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, bstart, status, int(p), n, L.num_tiles, dmask);
+            kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask);
     }
     return cudaGetLastError();
 }
@@ -105,13 +105,13 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     RSBD8G_MODE_SWITCH(mode, RSBD8G_HIST)
 #undef RSBD8G_HIST
     if (e != cudaSuccess) return e;
+    SortArrays arrs{};
+    arrs.p[kArrIn] = in;
+    arrs.p[kArrOut] = out;
+    arrs.p[kArrBuf] = buf;
+    arrs.p[kArrKeysA] = r.indirect ? scratch + L.keys_a : nullptr;
+    arrs.p[kArrKeysB] = r.indirect ? scratch + L.keys_b : nullptr;
     PlanArgs a{};
-    a.in = in;
-    a.out = out;
-    a.buf = buf;
-    a.keys_a = r.indirect ? scratch + L.keys_a : nullptr;
-    a.keys_b = r.indirect ? scratch + L.keys_b : nullptr;
-    a.elem_bytes = r.elem_bytes;
     a.inplace = inplace;
     a.to_buffer = to_buffer;
     a.rev = r.rev;
@@ -132,22 +132,22 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     const uint32_t P = uint32_t(KeyTraits<U>::kDigits);
     if (r.indirect) {
         e = L.wide_status
-                ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, 0u, s)
-                : launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint32_t>(P, n, L, scratch, 0u, s);
+                ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, arrs, 0u, s)
+                : launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint32_t>(P, n, L, scratch, arrs, 0u, s);
     } else if (L.wide_status) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint64_t>(P, n, L, scratch, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint64_t>(P, n, L, scratch, arrs, dmask, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else if (L.large_tiles) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gl.threads, gl.items, uint32_t>(P, n, L, scratch, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gl.threads, gl.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else if (L.small_tiles) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gs.threads, gs.items, uint32_t>(P, n, L, scratch, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gs.threads, gs.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint32_t>(P, n, L, scratch, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     }
@@ -157,7 +157,7 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     const uint32_t cgrid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(device_sms(dev)) * 8)));
     {
         LaunchTimer t(s, RSBD8G_KERNEL_COPY, uint32_t(sizeof(U)), 0, n);
-        k_copy<<<cgrid, 256, 0, s>>>(reinterpret_cast<const Control *>(scratch + L.ctrl), n);
+        k_copy<<<cgrid, 256, 0, s>>>(reinterpret_cast<Control *>(scratch + L.ctrl), arrs, n, uint32_t(r.elem_bytes));
     }
     return cudaGetLastError();
 }

@@ -51,6 +51,14 @@ class Server:
         self._keep = {}   # request id -> tensors kept alive until the request is done
 
     def submit(self, input, output, direction="ascfwdorder", mode="native", key_dtype=None) -> int:
+        """Queue one sort of `input` into `output`.  The server's streams are not ordered after the
+        caller's, so work still queued on the current stream (which may write the input, or have
+        used the arrays' memory before) is waited for on the host first."""
+        import torch
+        if hasattr(input, "device"):
+            cur = torch.cuda.current_stream(input.device)
+            if not cur.query():
+                cur.synchronize()
         d = api.make_desc(key_dtype if key_dtype is not None else input.dtype, direction, mode)
         rid = ctypes.c_uint64()
         api._check(_lib().rsbd8g_server_submit(self._h, ctypes.byref(d), api._count(input, None, d), api._ptr(input),

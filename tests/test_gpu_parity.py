@@ -155,6 +155,7 @@ def test_graph_capture_of_noalloc():
     inp, out, buf = to_dev(a), empty_dev(n, np.float32), empty_dev(n, np.float32)
     scratch = torch.empty(rs.scratch_bytes(np.float32, n, "dscfwdorder"), dtype=torch.uint8, device="cuda")
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())      # the arrays were made on the current stream
     g = torch.cuda.CUDAGraph()
     with torch.cuda.stream(s):
         rs.radixsortcopynoalloc(inp, out, buf, scratch, "dscfwdorder", key_dtype=np.float32, stream=s)

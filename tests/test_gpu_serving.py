@@ -91,3 +91,34 @@ def test_request_larger_than_budget_refused():
         with pytest.raises(api.RSBD8GError) as e:
             srv.submit(x, y, key_dtype=np.uint32)
         assert e.value.status == api.ERR_BUSY
+
+
+def test_sixteen_byte_keys_served_beside_other_requests():
+    """128-bit integer and binary128-float keys (held as pairs of 64-bit words) submitted among
+    4-byte requests: every result equals the oracle's sort of its input."""
+    import torch
+    from radixsortbidi8_gb300 import serving
+    lens = S.log_uniform_lengths(303, 40, 1 << 4, 1 << 17)
+    wide = [("u128", "native", "ascfwdorder"), ("i128", "native", "dscfwdorder"), ("f128", "nativeabs", "ascfwdorder")]
+    reqs = []
+    for i, m in enumerate(int(x) for x in lens):
+        if i % 2:
+            words = S.uniform_bits(400 + i, 2 * m, np.uint64)
+            words[2::10] = words[0]
+            words[3::10] = words[1]                  # repeated 128-bit keys
+            reqs.append(("wide", words) + wide[i % 3])
+        else:
+            reqs.append(("narrow", S.uniform_bits(400 + i, m, np.uint32), np.uint32, "native", "dscfwdorder"))
+    ins = [torch.from_numpy(r[1].view(np.int64 if r[0] == "wide" else np.int32).copy()).cuda() for r in reqs]
+    outs = [torch.empty_like(x) for x in ins]
+    with serving.Server(budget_bytes=1 << 30, max_inflight=4) as srv:
+        ids = [srv.submit(ins[i], outs[i], r[4], r[3], key_dtype=r[2]) for i, r in enumerate(reqs)]
+        srv.drain()
+        infos = [srv.wait(q) for q in ids]
+    assert all(x.status == 0 for x in infos)
+    for i, r in enumerate(reqs):
+        if r[0] == "wide":
+            got = outs[i].cpu().numpy().view(np.uint64)
+            assert same_bits(got, O.sortcopy_wide(r[1], r[2], r[3], r[4]).reshape(-1)), (i, r[2])
+        else:
+            assert same_bits(from_dev(outs[i], np.uint32), O.sortcopy(r[1], r[3], r[4])), i
