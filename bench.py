@@ -250,6 +250,9 @@ def gb300_arm(args, rank: int, world: int):
     serving = None
     if rank == 0 and world == 1 and not args.no_configs:
         serving = serving_run(args, 2000.0, 5.0, 2000, 0 if args.no_cpu else 32)
+        # near the server's capacity (about 36 GKeys/s offered): requests queue, and the waiting
+        # ones are coalesced into shared launches
+        serving["near_capacity"] = serving_run(args, 6000.0, 2.0, 0, 0 if args.no_cpu else 8)
     # correctness of the timed outputs: byte comparison with the oracle (the cpu_baseline leg's
     # checker, outside the timed region)
     check = "not checked (--no-cpu)" if args.no_cpu else verify_outputs(arrays, bufs)
@@ -880,8 +883,9 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     """Poisson arrivals at `rate` req/s for `duration` s; length log-uniform [2^10, 2^26]; key type
     uniform over {uint16, int32, float32, float64}; direction asc/desc (forward order); absolute filter
     with probability 0.5; 64 GB device budget.  Inputs are slices of device-resident pools (the loop
-    measures sort service, not host transfers).  Then the first `closed` requests, closed-loop: all
-    queued at once through the server vs a loop of plain allocating sorts.  `checks` served results
+    measures sort service, not host transfers).  Then (unless `closed` is 0) the first `closed`
+    requests, closed-loop: all queued at once through the server vs a loop of plain allocating
+    sorts.  `checks` served results
     (spread over the run, the largest request included) are compared with the oracle."""
     import numpy as np
     import torch
@@ -966,6 +970,15 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     srv.close()
     del rings
     torch.cuda.empty_cache()
+    open_loop = {"config": f"serving: Poisson {rate:g} req/s for {duration:g} s, lengths log-uniform "
+                           f"[2^10, 2^26], {{u16, i32, f32, f64}}, asc/desc, abs p=0.5, 64 GB budget",
+                 "requests": nreq, "offered_gkeys_s": round(float(lens.sum()) / duration / 1e9, 3),
+                 "served_gkeys_s": round(keys / (t_last - t_first) / 1e9, 3), "latency": lat,
+                 "batches": st["batches"], "launches_per_request": round(st["batches"] / max(1, nreq), 3),
+                 "max_coalesced": st["max_coalesced"], "max_inflight_batches": st["max_inflight_batches"],
+                 "checked": f"{len(pick) - bad} of {len(pick)} served results bit-exact vs oracle"}
+    if closed <= 0:
+        return open_loop
     # closed loop: a prefix of the same requests, queued at once vs a plain allocating-sort loop
     m_req = min(nreq, closed)
     outs = [torch.empty(int(lens[i]), dtype=kinds[kind[i]][1], device=dev) for i in range(m_req)]
@@ -1008,13 +1021,7 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     keys2 = int(lens[:m_req].sum())
     del outs
     torch.cuda.empty_cache()
-    return {"config": f"serving: Poisson {rate:g} req/s for {duration:g} s, lengths log-uniform "
-                      f"[2^10, 2^26], {{u16, i32, f32, f64}}, asc/desc, abs p=0.5, 64 GB budget",
-            "requests": nreq, "offered_gkeys_s": round(float(lens.sum()) / duration / 1e9, 3),
-            "served_gkeys_s": round(keys / (t_last - t_first) / 1e9, 3), "latency": lat,
-            "batches": st["batches"], "launches_per_request": round(st["batches"] / max(1, nreq), 3),
-            "max_coalesced": st["max_coalesced"], "max_inflight_batches": st["max_inflight_batches"],
-            "checked": f"{len(pick) - bad} of {len(pick)} served results bit-exact vs oracle",
+    return {**open_loop,
             "closed_loop": {"requests": m_req, "keys": keys2,
                             "served_gkeys_s": round(keys2 / served_s / 1e9, 3),
                             "plain_loop_gkeys_s": round(keys2 / loop_s / 1e9, 3),
