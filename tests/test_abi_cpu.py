@@ -113,3 +113,20 @@ def test_tile_tiers_follow_the_count():
     for n in ((1 << 23) - 1, 1 << 25):
         body = -(-n // 8192) * 8 * kib
         assert body <= rs.scratch_bytes(np.int64, n) < body + 128 * kib
+
+
+def test_sort_array_lookup_of_the_control_block_indices(tmp_path):
+    """The scatter and copy kernels find their arrays by index (rsbd8g::sort_array): valid indices,
+    the 'none' index, and indices that name no array (fallback + fault flag), checked on the host."""
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("no nvcc")
+    src = os.path.join(ROOT, "tests", "cpp", "sort_array_test.cu")
+    exe = str(tmp_path / "sort_array_test")
+    r = subprocess.run([nvcc, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "radixsortbidi8_gb300", "csrc"),
+                        src, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
