@@ -347,6 +347,14 @@ RSBD8G_API int rsbd8g_version(void);
  * Needs a device.  No counterpart in the reference. */
 RSBD8G_API rsbd8g_status rsbd8g_binary_version(int *version);
 
+/* Load and set up, on the current device, every kernel that sorts with this descriptor's key type,
+ * mode and indirection can launch, at any count (and, for direct keys, the segmented sort's).
+ * The CUDA runtime loads each kernel at its first use, which can hold the calling thread for tens
+ * of milliseconds; a latency-sensitive caller prepares its descriptors once ahead of its first
+ * sorts.  Optional: every entry point works without it.  rsbd8g_server_create prepares every key
+ * type and mode the server accepts.  Allocates nothing.  No counterpart in the reference. */
+RSBD8G_API rsbd8g_status rsbd8g_prepare(const rsbd8g_desc *desc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,7 @@ def lib():
         "rsbd8g_radixsortcopy_static": ([P, S, VP, VP, VP], I32),
         "rsbd8g_static_status": ([VP], I32),
         "rsbd8g_binary_version": ([ctypes.POINTER(I32)], I32),
+        "rsbd8g_prepare": ([ctypes.POINTER(Desc)], I32),
         "rsbd8g_merge_runs": ([P, S, ctypes.POINTER(ctypes.c_size_t), VP, VP, VP, VP], I32),
         "rsbd8g_radixsortcopy_chunked": ([P, S, VP, VP, S, VP], I32),
     }
@@ -320,6 +321,14 @@ def binary_version() -> int:
     v = ctypes.c_int(0)
     _check(lib().rsbd8g_binary_version(ctypes.byref(v)), "rsbd8g_binary_version")
     return v.value
+
+
+def prepare(key_dtype, direction="ascfwdorder", mode="native", indirection=DIRECT, offset1: int = 0,
+            offset2: int = 0) -> None:
+    """Load every kernel that sorts of this key type, mode and indirection can launch (rsbd8g_prepare),
+    so that the first sort does not wait for the CUDA runtime to load them."""
+    d = make_desc(key_dtype, direction, mode, indirection, offset1, offset2)
+    _check(lib().rsbd8g_prepare(ctypes.byref(d)), "rsbd8g_prepare")
 
 
 # ---- indirection --------------------------------------------------------------------------

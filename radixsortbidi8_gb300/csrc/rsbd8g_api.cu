@@ -280,6 +280,26 @@ RSBD8G_API rsbd8g_status rsbd8g_binary_version(int *version) {
     return RSBD8G_OK;
 }
 
+RSBD8G_API rsbd8g_status rsbd8g_prepare(const rsbd8g_desc *desc) {
+    Resolved r;
+    rsbd8g_status st = resolve(desc, &r);
+    if (st != RSBD8G_OK) return st;
+    cudaError_t e;
+    switch (r.key_bytes) {
+        case 1: e = launch_sort_k1_prepare(r); break;
+        case 2: e = launch_sort_k2_prepare(r); break;
+        case 4: e = launch_sort_k4_prepare(r); break;
+        case 8: e = launch_sort_k8_prepare(r); break;
+        default: e = r.x87 ? launch_sort_x87_prepare(r) : launch_sort_k16_prepare(r); break;
+    }
+    if (e == cudaSuccess && r.indirect == RSBD8G_DIRECT && !r.x87) e = prepare_segmented(r);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return RSBD8G_ERR_CUDA;
+    }
+    return RSBD8G_OK;
+}
+
 RSBD8G_API rsbd8g_status rsbd8g_profile_enable(int enable) { return profile_enable(enable); }
 
 RSBD8G_API rsbd8g_status rsbd8g_profile_collect(rsbd8g_launch_record *records, size_t capacity, size_t *count) {

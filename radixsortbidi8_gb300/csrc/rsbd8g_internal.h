@@ -53,7 +53,8 @@ int device_sms(int dev);
 // the launch sequence of one sort, per key size (rsbd8g_sort_k{1,2,4,8}.cu)
 #define RSBD8G_DECLARE_LAUNCH(name)                                                                          \
     cudaError_t name(const Resolved &r, uint64_t n, const Layout &L, unsigned char *scratch, const void *in, \
-                     void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);
+                     void *out, void *buf, bool inplace, bool to_buffer, cudaStream_t s);                   \
+    cudaError_t name##_prepare(const Resolved &r);   /* load every kernel this sort can launch */
 RSBD8G_DECLARE_LAUNCH(launch_sort_k1)
 RSBD8G_DECLARE_LAUNCH(launch_sort_k2)
 RSBD8G_DECLARE_LAUNCH(launch_sort_k4)
@@ -123,7 +124,8 @@ struct SegLayout {
 struct SegArgs;
 #define RSBD8G_DECLARE_SEG_LAUNCH(name)                                                                \
     cudaError_t name(const Resolved &r, const SegArgs &a, const SegLayout &L, unsigned char *scratch, \
-                     const void *in, void *out, void *buf, cudaStream_t s);
+                     const void *in, void *out, void *buf, cudaStream_t s);                           \
+    cudaError_t name##_prepare(const Resolved &r);   /* load every kernel this sort can launch */
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k1)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k2)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k4)
@@ -131,6 +133,7 @@ RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k8)
 RSBD8G_DECLARE_SEG_LAUNCH(launch_segmented_k16)
 
 rsbd8g_status resolve(const rsbd8g_desc *d, Resolved *r);
+cudaError_t prepare_segmented(const Resolved &r);   // rsbd8g_segmented_api.cu: rsbd8g_prepare's segmented part
 // p is device memory (cudaMalloc, a memory pool, a __device__ array); null counts as such
 bool device_memory(const void *p);
 // the resolved filter of a descriptor (isabsvalue | issignmode << 1 | isfltpmode << 2 | x87 << 3),

@@ -45,6 +45,16 @@ rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, cons
 }
 
 }  // namespace
+
+cudaError_t prepare_segmented(const Resolved &r) {
+    switch (r.key_bytes) {
+        case 1: return launch_segmented_k1_prepare(r);
+        case 2: return launch_segmented_k2_prepare(r);
+        case 4: return launch_segmented_k4_prepare(r);
+        case 8: return launch_segmented_k8_prepare(r);
+        default: return launch_segmented_k16_prepare(r);
+    }
+}
 }  // namespace rsbd8g
 
 using namespace rsbd8g;
