@@ -859,7 +859,8 @@ def batched_run(args, which: str, steps: int, check: bool) -> dict:
            "batched_gkeys_s": round(total / (ms * 1e-3) / 1e9, 3), "loop_ms": round(loop_ms, 2),
            "loop_gkeys_s": round(total / (loop_ms * 1e-3) / 1e9, 3),
            "speedup_vs_loop": round(loop_ms / ms, 2), "identical_to_loop": same,
-           "tuning": {"small_variant": sorter.tuning.small_variant, "small_cutoff": sorter.tuning.small_cutoff}}
+           "tuning": {"small_variant": sorter.tuning.small_variant, "small_cutoff": sorter.tuning.small_cutoff,
+                      "large_variant": sorter.tuning.large_variant}}
     if check:
         got = sorter.output.cpu().numpy().view(kdt)
         a = keys.cpu().numpy().view(kdt)

@@ -237,7 +237,8 @@ RSBD8G_API rsbd8g_status rsbd8g_radixsortcopy_chunked(const rsbd8g_desc *desc, s
 typedef struct rsbd8g_segtuning {
     uint32_t small_variant;   /* shape of the small-segment block sort: 0, 1 or 2 (threads x items of the block sort, per key size) */
     uint32_t small_cutoff;    /* largest segment sorted whole in shared memory (0 = the shape's capacity) */
-    uint32_t reserved[2];
+    uint32_t large_variant;   /* tile of the large segments' onesweep passes: 0 or 1 (keys per thread, per key size) */
+    uint32_t reserved;
 } rsbd8g_segtuning;
 
 RSBD8G_API rsbd8g_status rsbd8g_segmented_scratch_bytes(const rsbd8g_desc *desc, size_t total, size_t nsegs,

@@ -6,8 +6,9 @@ shared memory by a block-local radix sort, large ones run the onesweep passes, a
 launches (C ABI ``rsbd8g_segmented_sortcopy``).  ``SegmentedSorter`` owns the buffers of one
 batch shape and can capture the whole call into a CUDA graph (one graph launch per batch).
 
-The small-segment block-sort shape (threads x items) and the small/large cutoff are picked per key
-size by ``autotune`` and kept in ``tuning.json`` beside this file; ``tuning_for`` reads it.
+The small-segment block-sort shape (threads x items), the small/large cutoff and the tile of the
+large segments' onesweep passes (keys per thread) are picked per key size by ``autotune`` and kept
+in ``tuning.json`` beside this file; ``tuning_for`` reads it.
 """
 from __future__ import annotations
 
@@ -25,12 +26,15 @@ SMALL_SHAPES = {  # variant -> (threads, items) per key size, as compiled in the
     1: [(256, 8), (256, 16), (512, 16)], 2: [(256, 8), (256, 16), (512, 16)],
     4: [(256, 8), (256, 16), (512, 16)], 8: [(256, 8), (256, 12), (512, 12)],
 }
+LARGE_SHAPES = {  # large_variant -> (threads, items) of the large segments' onesweep tiles
+    1: [(512, 28), (512, 20)], 2: [(512, 28), (512, 20)], 4: [(512, 28), (512, 20)], 8: [(512, 12), (512, 16)],
+}
 
 
 class SegTuning(ctypes.Structure):
     """rsbd8g_segtuning of include/rsbd8g.h"""
     _fields_ = [("small_variant", ctypes.c_uint32), ("small_cutoff", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("large_variant", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 def _lib():
@@ -51,11 +55,12 @@ def _lib():
 
 
 def tuning_for(key_bytes: int) -> SegTuning:
-    """The tuned small-segment shape and cutoff for a key size (library defaults if untuned)."""
+    """The tuned small-segment shape, cutoff and large-segment tile for a key size (library defaults
+    if untuned)."""
     try:
         with open(TUNING_PATH) as f:
             t = json.load(f)["segmented"][str(key_bytes)]
-        return SegTuning(int(t["small_variant"]), int(t["small_cutoff"]))
+        return SegTuning(int(t["small_variant"]), int(t["small_cutoff"]), int(t.get("large_variant", 0)))
     except (OSError, KeyError, ValueError):
         return SegTuning(1, 0)
 
@@ -234,39 +239,55 @@ def _synthetic_batch(key_bytes: int, nsegs: int, lo: int, hi: int, seed: int, de
     return keys, torch.from_numpy(offs).to(device), offs
 
 
-def autotune(key_bytes_list=(2, 4, 8), nsegs: int = 20000, lo: int = 16, hi: int = 1 << 16, reps: int = 3,
-             write: bool = True) -> dict:
-    """Time every compiled small-segment shape and a few cutoffs on a synthetic log-uniform batch
-    per key size; keep the fastest in tuning.json."""
+def _time_sorter(keys, offs, kd, t: SegTuning, reps: int) -> float:
+    """ms per sort of the batch with tuning t"""
+    import torch
+    s = SegmentedSorter(keys, offs, key_dtype=kd, tuning=t)
+    torch.cuda.current_stream().synchronize()    # keys made, buffers allocated on this stream
+    with torch.cuda.stream(s.stream):
+        s.run()
+        s.stream.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            s.run()
+        s.stream.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    del s
+    return ms
+
+
+# the batch each key size is tuned on: (segments, shortest, longest), lengths log-uniform; keys up to
+# 4 bytes: the 2^28-key batch of uniform arrays of 16 to 2^20 keys, 8-byte keys: arrays of 64 to 2^18
+TUNE_BATCHES = {1: (3000, 16, 1 << 20), 2: (3000, 16, 1 << 20), 4: (3000, 16, 1 << 20), 8: (20000, 64, 1 << 18)}
+
+
+def autotune(key_bytes_list=(2, 4, 8), reps: int = 3, batches: dict | None = None, write: bool = True) -> dict:
+    """Per key size: time every compiled small-segment shape (threads x items) with a few cutoffs,
+    each with every compiled tile of the large segments' onesweep passes (keys per thread), on a
+    synthetic batch of log-uniform lengths (TUNE_BATCHES); the fastest settings go to tuning.json."""
     import torch
     kd = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+    shapes = batches if batches is not None else TUNE_BATCHES
     best = {}
     report = {}
     for kb in key_bytes_list:
+        nsegs, lo, hi = shapes[kb]
         keys, offs, _ = _synthetic_batch(kb, nsegs, lo, hi, seed=1234 + kb)
         results = []
         for v, (th, it) in enumerate(SMALL_SHAPES[kb]):
             cap = th * it
             for cutoff in sorted({cap // 4, cap // 2, cap}):
-                t = SegTuning(v, cutoff)
-                s = SegmentedSorter(keys, offs, key_dtype=kd[kb], tuning=t)
-                torch.cuda.current_stream().synchronize()    # keys made, buffers allocated on this stream
-                with torch.cuda.stream(s.stream):
-                    s.run()
-                    s.stream.synchronize()
-                    t0 = time.perf_counter()
-                    for _ in range(reps):
-                        s.run()
-                    s.stream.synchronize()
-                ms = (time.perf_counter() - t0) / reps * 1e3
-                results.append((ms, v, cutoff))
-                del s
+                for lv in range(len(LARGE_SHAPES[kb])):
+                    results.append((_time_sorter(keys, offs, kd[kb], SegTuning(v, cutoff, lv), reps), v, cutoff, lv))
         results.sort()
-        ms, v, cutoff = results[0]
-        best[str(kb)] = {"small_variant": v, "small_cutoff": cutoff, "threads_items": SMALL_SHAPES[kb][v],
-                         "ms": round(ms, 3)}
-        report[str(kb)] = [{"ms": round(m, 3), "small_variant": vv, "small_cutoff": cc} for m, vv, cc in results]
+        ms, v, cutoff, lv = results[0]
         del keys, offs
+        torch.cuda.empty_cache()
+        best[str(kb)] = {"small_variant": v, "small_cutoff": cutoff, "threads_items": SMALL_SHAPES[kb][v],
+                         "large_variant": lv, "large_threads_items": LARGE_SHAPES[kb][lv], "ms": round(ms, 3),
+                         "batch": {"segments": nsegs, "lengths": f"log-uniform [{lo}, {hi}]"}}
+        report[str(kb)] = [{"ms": round(m, 3), "small_variant": a, "small_cutoff": c, "large_variant": x}
+                           for m, a, c, x in results]
     if write:
         data = {}
         try:
@@ -275,7 +296,7 @@ def autotune(key_bytes_list=(2, 4, 8), nsegs: int = 20000, lo: int = 16, hi: int
         except (OSError, ValueError):
             pass
         data.setdefault("segmented", {}).update(best)
-        data["segmented_workload"] = {"nsegs": nsegs, "lengths": f"log-uniform [{lo}, {hi}]", "reps": reps}
+        data["segmented_workload"] = {"reps": reps, "batches": {str(k): list(v) for k, v in shapes.items()}}
         with open(TUNING_PATH, "w") as f:
             json.dump(data, f, indent=1)
     return {"best": best, "all": report}

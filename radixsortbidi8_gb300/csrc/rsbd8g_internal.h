@@ -84,11 +84,16 @@ constexpr SweepGeometry sweep_geometry_large(int key_bytes) {
 constexpr SweepGeometry sweep_geometry_small(int key_bytes) {
     return key_bytes <= 4 ? SweepGeometry{512, 16} : sweep_geometry(key_bytes, false);
 }
-// the segmented sort's large segments: 8-byte keys take smaller tiles than the plain sort (a
-// segment's last tile is partly empty, and large 8-byte segments are the shorter ones); keys up to
-// 4 bytes take 512 x 28 (measured against 24 and 32 on the 2^28-key batch of uint32 arrays)
-constexpr SweepGeometry seg_sweep_geometry(int key_bytes) {
-    return SweepGeometry{512, key_bytes == 16 ? 6 : (key_bytes == 8 ? 12 : 28)};
+// the segmented sort's large segments, two tile sizes per key size, picked per batch shape by the
+// autotuner (rsbd8g_segtuning::large_variant).  Variant 0: 512 x 28 for keys up to 4 bytes (measured
+// against 24 and 32 on the 2^28-key batch of uint32 arrays) and 512 x 12 for 8-byte keys, smaller
+// than the plain sort's tiles because a segment's last tile is partly empty.  Variant 1: 512 x 20
+// and 512 x 16, for batches of shorter or longer large segments.  16-byte keys: 512 x 6 in both.
+constexpr int kSegLargeVariants = 2;
+constexpr SweepGeometry seg_sweep_geometry(int key_bytes, int variant) {
+    return SweepGeometry{512, key_bytes == 16 ? 6
+                              : key_bytes == 8 ? (variant == 1 ? 16 : 12)
+                                               : (variant == 1 ? 20 : 28)};
 }
 
 #define RSBD8G_MODE_SWITCH(mode, CALL) \
@@ -118,7 +123,7 @@ constexpr int kSegSmallVariants = 3;
 struct SegLayout {
     size_t ctrl, large_seg, large_tbase, small_seg, seg_hist, seg_mask, tile_seg, status, status_bytes, zero_bytes, total;
     uint64_t nlarge_max, tiles_max;
-    uint32_t cutoff, small_variant, tile;
+    uint32_t cutoff, small_variant, tile, large_variant;
 };
 
 struct SegArgs;

@@ -154,9 +154,12 @@ cudaError_t launch_segmented_mode_t(const Resolved &r, const SegArgs &a, const S
         k_seg_plan<<<g, 256, 0, s>>>(a, KeyTraits<U>::kDigits);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    constexpr SweepGeometry gd = seg_sweep_geometry(int(sizeof(U)));
+    constexpr SweepGeometry g0 = seg_sweep_geometry(int(sizeof(U)), 0), g1 = seg_sweep_geometry(int(sizeof(U)), 1);
     const uint32_t stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) ? 1u : 0xFFFFFFFFu;
-    e = launch_seg_sweeps_t<U, MODE, gd.threads, gd.items>(a, L, scratch, in, out, buf, stall, s);
+    if (L.large_variant == 1 && g1.items != g0.items)
+        e = launch_seg_sweeps_t<U, MODE, g1.threads, g1.items>(a, L, scratch, in, out, buf, stall, s);
+    else
+        e = launch_seg_sweeps_t<U, MODE, g0.threads, g0.items>(a, L, scratch, in, out, buf, stall, s);
     if (e != cudaSuccess) return e;
     {
         LaunchTimer t(s, RSBD8G_KERNEL_COPY, uint32_t(sizeof(U)), 0, a.nsegs);
@@ -181,12 +184,13 @@ template <typename U, int MODE>
 cudaError_t prepare_segmented_mode_t(int dev) {
     constexpr SegSmallShape sh0 = seg_small_shape(int(sizeof(U)), 0), sh1 = seg_small_shape(int(sizeof(U)), 1),
                             sh2 = seg_small_shape(int(sizeof(U)), 2);
-    constexpr SweepGeometry gd = seg_sweep_geometry(int(sizeof(U)));
+    constexpr SweepGeometry g0 = seg_sweep_geometry(int(sizeof(U)), 0), g1 = seg_sweep_geometry(int(sizeof(U)), 1);
     small_setup<U, MODE, sh0.threads, sh0.items>(dev);
     small_setup<U, MODE, sh1.threads, sh1.items>(dev);
     small_setup<U, MODE, sh2.threads, sh2.items>(dev);
     seg_hist_setup<U, MODE>(dev);
-    SegSweepKernels<U, MODE, gd.threads, gd.items>::setup(dev, nullptr, nullptr);
+    SegSweepKernels<U, MODE, g0.threads, g0.items>::setup(dev, nullptr, nullptr);
+    SegSweepKernels<U, MODE, g1.threads, g1.items>::setup(dev, nullptr, nullptr);
     cudaFuncAttributes fa{};
     cudaFuncGetAttributes(&fa, k_seg_classify);
     cudaFuncGetAttributes(&fa, k_seg_plan);

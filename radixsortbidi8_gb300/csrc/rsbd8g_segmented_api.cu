@@ -22,10 +22,13 @@ rsbd8g_status seg_layout(const Resolved &r, uint64_t total, uint64_t nsegs, cons
     const uint32_t cap = uint32_t(sh.threads * sh.items);
     const uint32_t cutoff = (t && t->small_cutoff) ? t->small_cutoff : cap;
     if (cutoff > cap) return RSBD8G_ERR_BAD_ARG;
-    const SweepGeometry g = seg_sweep_geometry(int(r.key_bytes));
+    const uint32_t lvariant = t ? t->large_variant : 0u;
+    if (lvariant >= uint32_t(kSegLargeVariants)) return RSBD8G_ERR_BAD_ARG;
+    const SweepGeometry g = seg_sweep_geometry(int(r.key_bytes), int(lvariant));
     L->tile = uint32_t(g.threads * g.items);
     L->cutoff = cutoff;
     L->small_variant = variant;
+    L->large_variant = lvariant;
     L->nlarge_max = std::max<uint64_t>(1, std::min<uint64_t>(nsegs, total / (uint64_t(cutoff) + 1)));
     L->tiles_max = total / L->tile + L->nlarge_max + 1;
     if (L->tiles_max >= (uint64_t(1) << 32) || nsegs >= (uint64_t(1) << 32)) return RSBD8G_ERR_TOO_LARGE;

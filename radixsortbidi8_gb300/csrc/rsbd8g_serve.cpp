@@ -262,7 +262,7 @@ struct Server {
             }
             if (take.empty()) return nullptr;    // memory is full: wait for a batch to finish
             size_t sb = 0;
-            rsbd8g_segtuning tun{1, 0, {0, 0}};
+            rsbd8g_segtuning tun{1, 0, 0, 0};
             const size_t n = take.size();
             const size_t tb = aup((n + 1) * 8) + 3 * aup(n * 8) + aup(n);
             size_t soff = 0, toff = 0;
@@ -342,7 +342,7 @@ struct Server {
         uint64_t *d_buf = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8) + 2 * aup(n * 8));
         uint8_t *d_dir = dt + aup((n + 1) * 8) + 3 * aup(n * 8);
         cudaStream_t s = streams[size_t(b->slot)];
-        rsbd8g_segtuning tun{1, 0, {0, 0}};
+        rsbd8g_segtuning tun{1, 0, 0, 0};
         rsbd8g_status st = RSBD8G_OK;
         *b->host_err = 0;
         if (b->big) {   // one request alone: the plain sort (its status word is at the scratch start too)
@@ -450,7 +450,7 @@ RSBD8G_API rsbd8g_status rsbd8g_server_submit(rsbd8g_server *h, const rsbd8g_des
                                               const void *input, void *output, uint64_t *request_id) {
     if (!h || !desc || !request_id) return RSBD8G_ERR_BAD_ARG;
     size_t probe = 0;
-    rsbd8g_segtuning tun{1, 0, {0, 0}};
+    rsbd8g_segtuning tun{1, 0, 0, 0};
     rsbd8g_status st = rsbd8g_segmented_scratch_bytes(desc, count ? count : 1, 1, &tun, &probe);
     if (st != RSBD8G_OK) return st;
     if (count >= (size_t(1) << 30)) return RSBD8G_ERR_TOO_LARGE;

@@ -124,15 +124,38 @@ def test_segmented_lookback_timeout_reported():
     _check(a, offs, np.uint32, "native", "ascfwdorder")
 
 
+@pytest.mark.parametrize("large_variant", [0, 1])
 @pytest.mark.parametrize("dt,mode,direction", [(np.uint32, "native", "dscrevorder"), (np.float64, "nativeabs", "ascrevorder")])
-def test_segmented_pipelined_pass_matches_oracle(dt, mode, direction):
+def test_segmented_pipelined_pass_matches_oracle(dt, mode, direction, large_variant):
     """A batch with tiles enough for the pipelined segmented pass (more than two per resident CTA):
     large segments of uneven sizes, small ones between them, consecutive tiles of one CTA crossing
-    segment boundaries."""
+    segment boundaries; both compiled tiles of the large segments."""
+    from radixsortbidi8_gb300 import batched as B
     rng_lens = [1 << 20, 3, 700001, 0, 5000, (1 << 20) + 77, 12289, 1, 900007, 65536, 2 ** 19 + 5, 44444]
     lens = rng_lens * 2
     a, offs = _segments(lens, dt, 31)
-    _check(a, offs, dt, mode, direction)
+    _check(a, offs, dt, mode, direction, B.SegTuning(1, 0, large_variant))
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float64], ids=lambda x: x.__name__)
+def test_segmented_second_large_tile_matches_oracle(dt):
+    """large_variant 1 (512 x 20 keys up to 4 bytes, 512 x 16 for 8-byte keys) at its tile edges"""
+    from radixsortbidi8_gb300 import batched as B
+    kb = np.dtype(dt).itemsize
+    th, it = B.SMALL_SHAPES[kb][1]
+    lth, lit = B.LARGE_SHAPES[kb][1]
+    a, offs = _segments(_lens_mixed(th * it, lth * lit), dt, 50 + kb)
+    for d in DIRS:
+        _check(a, offs, dt, "native", d, B.SegTuning(1, 0, 1))
+
+
+def test_segmented_rejects_an_unknown_large_tile():
+    import torch
+    from radixsortbidi8_gb300 import api, batched as B
+    with pytest.raises(api.RSBD8GError) as e:
+        B.segmented_scratch_bytes(np.uint32, 1000, 2, tuning=B.SegTuning(1, 0, 2))
+    assert e.value.status == api.ERR_BAD_ARG
+    del torch
 
 
 @pytest.mark.parametrize("flags", [0, 4])
