@@ -185,20 +185,57 @@ __global__ void __launch_bounds__(THREADS) k_seg_hist(SegArgs a, const U *__rest
         for (uint32_t x = gt + threadIdx.x; x < tend; x += THREADS) a.tile_seg[x] = idx;
         const uint64_t k0 = uint64_t(gt - a.large_tbase[idx]) * a.tile;
         const uint64_t k1 = min(len, uint64_t(tend - a.large_tbase[idx]) * a.tile);
-        constexpr int UNR = 8;                           // loads in flight per thread
-        for (uint64_t b = k0 + threadIdx.x; b < k1; b += uint64_t(THREADS) * UNR) {
-            U raw[UNR];
+        auto count = [&](U raw) {
+            const U k = filter_key<MODE>(raw);
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) {
-                const uint64_t i = b + uint64_t(u) * THREADS;
-                raw[u] = i < k1 ? src[i] : U{};
+            for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dm)) * C, 1u);
+        };
+        if constexpr (sizeof(U) < 16) {
+            // 16-byte loads over the aligned middle of [k0, k1) (as in k_histogram); the keys before
+            // the first 16-byte boundary and after the last whole vector by the first warp
+            constexpr int V = 16 / int(sizeof(U));
+            const U *base = src + k0;
+            const uint64_t cnt = k1 > k0 ? k1 - k0 : 0;
+            const uint64_t mis = (reinterpret_cast<uintptr_t>(base) & 15u) / sizeof(U);
+            const uint64_t head = mis ? (uint64_t(V) - mis < cnt ? uint64_t(V) - mis : cnt) : 0;
+            const uint64_t nvec = (cnt - head) / V;
+            const uint64_t tail0 = head + nvec * V;
+            if (threadIdx.x < 32) {
+                for (uint64_t i = threadIdx.x; i < head; i += 32) count(base[i]);
+                for (uint64_t i = tail0 + threadIdx.x; i < cnt; i += 32) count(base[i]);
             }
+            const uint4 *vp = reinterpret_cast<const uint4 *>(base + head);
+            constexpr int UNR = 4;                       // 16-byte loads in flight per thread
+            for (uint64_t b = threadIdx.x; b < nvec; b += uint64_t(THREADS) * UNR) {
+                uint4 v[UNR];
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) {
-                if (b + uint64_t(u) * THREADS >= k1) break;
-                const U k = filter_key<MODE>(raw[u]);
+                for (int u = 0; u < UNR; ++u) {
+                    const uint64_t j = b + uint64_t(u) * THREADS;
+                    v[u] = j < nvec ? __ldg(vp + j) : make_uint4(0, 0, 0, 0);
+                }
 #pragma unroll
-                for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dm)) * C, 1u);
+                for (int u = 0; u < UNR; ++u) {
+                    if (b + uint64_t(u) * THREADS >= nvec) break;
+                    U kk[V];
+                    memcpy(kk, &v[u], 16);
+#pragma unroll
+                    for (int q = 0; q < V; ++q) count(kk[q]);
+                }
+            }
+        } else {
+            constexpr int UNR = 8;                       // loads in flight per thread
+            for (uint64_t b = k0 + threadIdx.x; b < k1; b += uint64_t(THREADS) * UNR) {
+                U raw[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    const uint64_t i = b + uint64_t(u) * THREADS;
+                    raw[u] = i < k1 ? src[i] : U{};
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    if (b + uint64_t(u) * THREADS >= k1) break;
+                    count(raw[u]);
+                }
             }
         }
         __syncthreads();
