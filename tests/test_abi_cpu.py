@@ -130,3 +130,20 @@ def test_sort_array_lookup_of_the_control_block_indices(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+def test_prepare_and_tuning_refusals_without_a_device():
+    """rsbd8g_prepare refuses a bad descriptor before touching the device; the segmented scratch
+    sizing refuses a small shape or large-segment tile that was not compiled."""
+    L = rs.lib()
+    L.rsbd8g_prepare.argtypes = [ctypes.POINTER(api.Desc)]
+    L.rsbd8g_prepare.restype = ctypes.c_int
+    assert L.rsbd8g_prepare(None) == api.ERR_BAD_ARG
+    for kb, kind, mode in [(3, 0, 64), (4, 0, 9), (2, 2, 64), (4, 7, 64)]:
+        assert L.rsbd8g_prepare(ctypes.byref(api.Desc(kb, kind, mode, 0, 0, 0, 0, 0))) == api.ERR_BAD_ARG
+    from radixsortbidi8_gb300 import batched as B
+    for t in (B.SegTuning(3, 0, 0), B.SegTuning(1, 0, 2), B.SegTuning(1, 1 << 20, 0)):
+        with pytest.raises(api.RSBD8GError) as e:
+            B.segmented_scratch_bytes(np.uint32, 100000, 20, tuning=t)
+        assert e.value.status == api.ERR_BAD_ARG
+    assert B.segmented_scratch_bytes(np.uint32, 100000, 20, tuning=B.SegTuning(1, 0, 1)) > 0

@@ -149,15 +149,6 @@ def test_segmented_second_large_tile_matches_oracle(dt):
         _check(a, offs, dt, "native", d, B.SegTuning(1, 0, 1))
 
 
-def test_segmented_rejects_an_unknown_large_tile():
-    import torch
-    from radixsortbidi8_gb300 import api, batched as B
-    with pytest.raises(api.RSBD8GError) as e:
-        B.segmented_scratch_bytes(np.uint32, 1000, 2, tuning=B.SegTuning(1, 0, 2))
-    assert e.value.status == api.ERR_BAD_ARG
-    del torch
-
-
 @pytest.mark.parametrize("flags", [0, 4])
 def test_segmented_pointer_tables_match_oracle(flags):
     """The pointer-table form (one separate device array per segment) with and without
