@@ -20,6 +20,8 @@ configurations it is measured on):
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 GOLDEN = np.uint64(0x9E3779B97F4A7C15)
@@ -42,22 +44,25 @@ def unit_interval(bits: np.ndarray) -> np.ndarray:
     return ((bits >> np.uint64(11)).astype(np.float64) + 1.0) * (1.0 / 9007199254740992.0)
 
 
-def uniform_bits(seed: int, n: int, dtype) -> np.ndarray:
+# Every generator below is a function of the element index (counter-based), so `offset` gives
+# elements offset..offset+n-1 of the same sequence: host_parallel fills one array from chunks.
+
+def uniform_bits(seed: int, n: int, dtype, offset: int = 0) -> np.ndarray:
     dt = np.dtype(dtype)
     ut = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[dt.itemsize]
-    return splitmix64(seed, n).astype(ut).view(dt)
+    return splitmix64(seed, n, offset).astype(ut).view(dt)
 
 
-def low_bits_u32(seed: int, n: int, bits: int = 12) -> np.ndarray:
-    return (splitmix64(seed, n) & np.uint64((1 << bits) - 1)).astype(np.uint32)
+def low_bits_u32(seed: int, n: int, bits: int = 12, offset: int = 0) -> np.ndarray:
+    return (splitmix64(seed, n, offset) & np.uint64((1 << bits) - 1)).astype(np.uint32)
 
 
-def normal(seed: int, n: int, stream: int = 0) -> np.ndarray:
+def normal(seed: int, n: int, stream: int = 0, offset: int = 0) -> np.ndarray:
     """Approximately N(0, 1): the Irwin-Hall sum of 12 uniforms minus 6 (summed in a fixed order,
     so every platform rounds identically)."""
     acc = np.zeros(n, dtype=np.float64)
     for k in range(12):
-        acc += unit_interval(splitmix64(seed, n, stream=100 * stream + k + 1))
+        acc += unit_interval(splitmix64(seed, n, offset, stream=100 * stream + k + 1))
     return acc - 6.0
 
 
@@ -73,11 +78,11 @@ def exp2_det(t: np.ndarray) -> np.ndarray:
     return np.ldexp(p, i.astype(np.int64))
 
 
-def float_specials(seed: int, n: int, dtype=np.float32, sigma: float = 1e3) -> np.ndarray:
+def float_specials(seed: int, n: int, dtype=np.float32, sigma: float = 1e3, offset: int = 0) -> np.ndarray:
     """N(0, sigma) with 1% -0.0, 0.5% +-inf (half each sign), 0.1% NaN (half each sign)."""
     dt = np.dtype(dtype)
-    x = (normal(seed, n) * sigma).astype(dt)
-    r = unit_interval(splitmix64(seed, n, stream=7))
+    x = (normal(seed, n, offset=offset) * sigma).astype(dt)
+    r = unit_interval(splitmix64(seed, n, offset, stream=7))
     x[r <= 0.01] = -0.0
     inf = (r > 0.01) & (r <= 0.015)
     x[inf & (r <= 0.0125)] = np.inf
@@ -90,6 +95,23 @@ def float_specials(seed: int, n: int, dtype=np.float32, sigma: float = 1e3) -> n
     bits[nan & (r <= 0.0155)] = ut(qnan)
     bits[nan & (r > 0.0155)] = ut(qnan | sbit)
     return x
+
+
+def host_parallel(gen, n: int, out_dtype, *args, chunk: int = 1 << 22, threads: int | None = None,
+                  **kw) -> np.ndarray:
+    """gen(*args, m, ..., offset=o) for chunks of m elements, filled into one array by a thread pool
+    (the numpy operations release the interpreter lock); equal to one call of gen over n elements.
+    `args` are the arguments before the count (the seed), `kw` those after it."""
+    import concurrent.futures as cf
+    out = np.empty(n, dtype=out_dtype)
+
+    def fill(o):
+        m = min(chunk, n - o)
+        out[o:o + m] = gen(*args, m, offset=o, **kw)
+
+    with cf.ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        list(ex.map(fill, range(0, n, chunk)))
+    return out
 
 
 def records24(seed: int, n: int) -> np.ndarray:

@@ -283,3 +283,15 @@ def test_batched_oracle_equals_one_sort_per_array():
         items = [(a[offs[i]:offs[i + 1]], mode, d) for i in range(len(lens))]
         for g, (x, m, dd) in zip(O.sortcopy_batch(items, threads=3), items):
             assert np.array_equal(g.view(np.uint8), O.sortcopy(x, m, dd).view(np.uint8))
+
+
+def test_host_parallel_generation_equals_one_call():
+    """the benchmark's host arrays filled chunk by chunk in threads equal one serial call"""
+    from radixsortbidi8_gb300 import synth as S
+    n = 3 * 4096 + 17
+    for gen, args, kw, dt in ((S.float_specials, (5,), {"dtype": np.float64}, np.float64),
+                              (S.uniform_bits, (6,), {"dtype": np.int16}, np.int16),
+                              (S.low_bits_u32, (7,), {}, np.uint32)):
+        a = gen(*args, n, **kw)
+        b = S.host_parallel(gen, n, dt, *args, chunk=4096, threads=3, **kw)
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), gen.__name__
