@@ -8,7 +8,8 @@ run on the host copy of the same input:
     ascending, the exact pointer order (ties included);
   * the batched sort: every segment of the 2^28-key uint32 batch and of the float64 batch;
   * the serving loop: every request of a run of the serving configuration's request stream.
-Inputs are built on the device with the generators the benchmark uses (synth.py)."""
+Inputs are built on the device with the generators the benchmark uses (synth.py).  Two more cases
+sort 2^30 + 12345 keys, past the size where the look-back words widen to 8 bytes."""
 import os
 
 import numpy as np
@@ -20,6 +21,7 @@ from radixsortbidi8_gb300 import synth as S
 pytestmark = [pytest.mark.gpu, pytest.mark.timeout(1200)]
 
 THREADS = os.cpu_count() or 1
+SWEEP_SEED_WIDE = 0x5EED0030
 
 
 def _host(t, dtype) -> np.ndarray:
@@ -139,3 +141,27 @@ def test_served_requests_of_the_serving_stream_match_oracle():
     want = O.sortcopy_batch([(host_in[i], metas[i][2], metas[i][1]) for i in range(nreq)], threads=THREADS)
     bad = [i for i in range(nreq) if not _bytes_equal(got[i], want[i])]
     assert not bad, bad[:10]
+
+
+@pytest.mark.parametrize("name,kdt,mode,direction", [("uint32", np.uint32, "native", "ascfwdorder"),
+                                                     ("float32_abs", np.float32, "nativeabs", "dscrevorder"),
+                                                     ("int64", np.int64, "native", "dscfwdorder")])
+def test_past_2p30_keys_with_wide_lookback_words_matches_oracle(name, kdt, mode, direction):
+    """2^30 + 12345 keys: at 2^30 keys and more the look-back words widen to 8 bytes (62-bit counts)
+    and the offsets of the write-out to 64 bits; the last tile is partly empty.  The float32 case
+    also reads its first pass back to front (dscrevorder under the absolute filter)."""
+    import torch
+    import radixsortbidi8_gb300 as rs
+    n = (1 << 30) + 12345
+    kb = np.dtype(kdt).itemsize
+    bits = (S.float_specials_torch(SWEEP_SEED_WIDE, n, kb) if kdt == np.float32
+            else S.uniform_bits_torch(SWEEP_SEED_WIDE, n, kb))
+    out, buf = torch.empty_like(bits), torch.empty_like(bits)
+    scr = torch.empty(rs.scratch_bytes(kdt, n, direction, mode), dtype=torch.uint8, device=bits.device)
+    rs.radixsortcopynoalloc(bits, out, buf, scr, direction, mode, key_dtype=kdt)
+    assert rs.scratch_status(scr) == 0
+    a = _host(bits, kdt)
+    got = _host(out, kdt)
+    del bits, out, buf, scr
+    torch.cuda.empty_cache()
+    assert _bytes_equal(got, O.sortcopy(a, mode, direction, threads=THREADS))
