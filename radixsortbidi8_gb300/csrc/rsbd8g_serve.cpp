@@ -7,9 +7,11 @@
 // every request one segment, each in its own arrays, with its own direction), and launches each
 // batch on its own stream, so batches overlap on the device while new requests keep arriving.  A
 // request large enough to run alone goes through the plain sort (rsbd8g_radixsortcopynoalloc),
-// which is 13-18 % faster than the segmented launch on one large array.  The budget is one device arena allocated up front: the ping-pong
-// buffers, the batch scratch and the batch's pointer tables are carved out of it and given back
-// when the batch completes, so keys and scratch stay resident and nothing is allocated per request.
+// which is 13-18 % faster than the segmented launch on one large array.  The budget is one device
+// arena allocated up front: the ping-pong buffers, the batch scratch and the batch's pointer tables
+// are carved out of it and given back when the batch completes, so keys and scratch stay resident
+// and nothing is allocated per request.  Creating a server loads every kernel a request can need
+// (rsbd8g_prepare), so no request waits for the CUDA runtime to load one.
 // Completion is observed with a host function queued behind each batch on its stream.
 #include <cuda_runtime.h>
 
