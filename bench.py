@@ -265,11 +265,13 @@ def gb300_arm(args, rank: int, world: int):
     # per-sort and per-kernel breakdown from the launch records (launch order is fixed per step)
     per_sort = {nm: {"ms": 0.0, "sweep_ms": [], "launches": 0} for nm, *_ in arrays}
     ours = [r for r in recs if r["kernel"] != "memset"]
-    order = []
-    for nm, bits, *_ in arrays:
-        order += [nm] * (3 + 1 + bits.element_size())  # memset, histogram, plan, passes, copy
-    for i, r in enumerate(recs):
-        nm = order[i % len(order)]
+    # every sort's launches start with its memset; the sorts of a step run in the arrays' order
+    names = [nm for nm, *_ in arrays]
+    sort_i = -1
+    for r in recs:
+        if r["kernel"] == "memset":
+            sort_i += 1
+        nm = names[max(sort_i, 0) % len(names)]
         per_sort[nm]["ms"] += r["ms"]
         if r["kernel"] != "memset":
             per_sort[nm]["launches"] += 1

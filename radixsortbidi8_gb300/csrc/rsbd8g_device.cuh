@@ -88,6 +88,8 @@ struct Control {
     uint32_t copy_dst;
     uint32_t stall_tile;   // diagnostics: this tile never publishes (0xFFFFFFFF = off)
     uint32_t prefetch;     // 1: every array is device memory, so tiles may be prefetched into L2
+    uint32_t hist_done;    // histogram CTAs finished (the last one computes the plan)
+    uint32_t pad0;
     uint64_t spin_limit_ns;
     PassPlan plan[kMaxPasses];
 };

@@ -4,9 +4,10 @@
 //                                      shared-memory atomics on per-lane-class counters (direct
 //                                      keys) or warp-aggregated atomics on sub-histogram copies
 //                                      (the gather form, which reads the key through each object
-//                                      pointer and writes the filtered keys once)
-//   k_plan                             exclusive scan of every digit histogram, the reference's
-//                                      pass-skip test, and the ping-pong plan of the passes
+//                                      pointer and writes the filtered keys once); the CTA that
+//                                      finishes last runs plan_body: the exclusive scan of every
+//                                      digit histogram, the reference's pass-skip test and the
+//                                      ping-pong plan of the passes
 //   k_onesweep                         one stable scatter pass of a surviving digit: persistent
 //                                      CTAs claim tiles in order, rank keys with a warp
 //                                      multisplit (TileRank: shared-memory match words), resolve
@@ -16,163 +17,13 @@
 //   k_onesweep_pipe                    the same pass with the look-back of one tile overlapping the
 //                                      load and ranking of the next, and the next tile prefetched
 //                                      into L2 (the pass of every sort of two tiles per CTA or more)
-//   k_copy                             the plain / reversed copy when parity or all-skipped
-//                                      passes need one
+//   k_copy                             the plain / reversed copy of the in-place forms when parity
+//                                      or all-skipped passes need one (the copy forms need one only
+//                                      when every pass was skipped, and the last pass's launch does it)
 #pragma once
 #include "rsbd8g_device.cuh"
 
 namespace rsbd8g {
-
-// ---- up-front histograms --------------------------------------------------------------------
-
-// Gather-histogram counting: each CTA keeps kHistCopies sub-histograms (P digits x 256 bins, u32)
-// in shared memory and its warps spread over them, so warps rarely collide on a bin.  A warp whose
-// lanes all share the digit (a skewed digit, e.g. the zero top bytes of small keys) adds 32 with
-// one atomic instead of 32 conflicting ones.
-constexpr int kHistCopies = 4;
-
-__device__ __forceinline__ void hist_add(uint32_t *h, uint32_t d, bool valid) {
-    const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
-    const bool v0 = __shfl_sync(0xFFFFFFFFu, valid, 0);
-    if (__all_sync(0xFFFFFFFFu, valid && d == d0)) {
-        if ((threadIdx.x & 31u) == 0 && v0) atomicAdd(h + d0, 32u);
-    } else if (valid) {
-        atomicAdd(h + d, 1u);
-    }
-}
-
-template <typename U>
-__device__ __forceinline__ void count_key(uint32_t *sh, U k, bool valid, uint32_t dmask) {
-#pragma unroll
-    for (int p = 0; p < KeyTraits<U>::kDigits; ++p) hist_add(sh + p * kBuckets, digit_of(k, p) ^ dmask, valid);
-}
-
-// copies of the gather histogram: fewer for the 16 digits of 128-bit keys (static shared memory)
-template <int P>
-constexpr int gather_hist_copies() { return P > 8 ? 2 : kHistCopies; }
-
-template <int THREADS, int P>
-__device__ __forceinline__ void zero_hist(uint32_t *sh) {
-    for (int i = threadIdx.x; i < gather_hist_copies<P>() * P * kBuckets; i += THREADS) sh[i] = 0;
-    __syncthreads();
-}
-
-template <int THREADS, int P>
-__device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long long *ghist) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
-        uint32_t v = 0;
-#pragma unroll
-        for (int c = 0; c < gather_hist_copies<P>(); ++c) v += sh[c * P * kBuckets + i];
-        if (v) atomicAdd(ghist + i, (unsigned long long)v);
-    }
-}
-
-// Direct keys: all P digit histograms in one read.  Every (digit position, bin) has C shared-memory
-// counters, one per lane class (lane % C), laid out so that lane l always uses bank l % 32: the 32
-// lanes of a warp never meet in a bank (C = 32, keys up to 4 bytes) or at most pairwise (C = 16,
-// 8-byte keys, 128 KB either way).  One 1024-thread CTA per SM reads 16-byte vectors grid-strided;
-// at the end each CTA folds its C copies (rotated reads, conflict-free) into the global histogram.
-template <int P>
-constexpr int hist_lane_copies() { return P <= 4 ? 32 : (P <= 8 ? 16 : 8); }
-
-template <typename U, int MODE, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, uint32_t dmask,
-                                                       unsigned long long *__restrict__ ghist) {
-    constexpr int P = KeyTraits<U>::kDigits;
-    constexpr int C = hist_lane_copies<P>();
-    constexpr int V = 16 / int(sizeof(U));
-    extern __shared__ __align__(16) uint32_t shl[];
-    for (int i = threadIdx.x; i < C * P * kBuckets; i += THREADS) shl[i] = 0;
-    __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t *sh = shl + (lane & uint32_t(C - 1));
-    auto count = [&](U k, bool ok) {
-        if (!ok) return;
-#pragma unroll
-        for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dmask)) * C, 1u);
-    };
-    const uint64_t mis = (reinterpret_cast<uintptr_t>(keys) & 15u) / sizeof(U);
-    const uint64_t head = mis ? (uint64_t(V) - mis < n ? uint64_t(V) - mis : n) : 0;
-    const uint64_t nvec = (n - head) / V;
-    const uint64_t tail0 = head + nvec * V;
-    const uint64_t gthread = uint64_t(blockIdx.x) * THREADS + threadIdx.x;
-    const uint64_t nthreads = uint64_t(gridDim.x) * THREADS;
-    if (gthread < 32) {
-        for (uint64_t i = gthread; i < head; i += 32) count(filter_key<MODE>(keys[i]), true);
-        for (uint64_t i = tail0 + gthread; i < n; i += 32) count(filter_key<MODE>(keys[i]), true);
-    }
-    const uint4 *kv = reinterpret_cast<const uint4 *>(keys + head);
-    constexpr int UNR = 4;
-    for (uint64_t b = gthread; b < nvec; b += nthreads * UNR) {
-        uint4 v[UNR];
-#pragma unroll
-        for (int u = 0; u < UNR; ++u) {
-            const uint64_t i = b + uint64_t(u) * nthreads;
-            v[u] = i < nvec ? __ldg(kv + i) : make_uint4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int u = 0; u < UNR; ++u) {
-            const bool ok = b + uint64_t(u) * nthreads < nvec;
-            U k[V];
-            memcpy(k, &v[u], 16);
-#pragma unroll
-            for (int j = 0; j < V; ++j) count(filter_key<MODE>(k[j]), ok);
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
-        uint32_t t = 0;
-#pragma unroll 8
-        for (int c = 0; c < C; ++c) t += shl[i * C + ((c + i) & (C - 1))];
-        if (t) atomicAdd(ghist + i, (unsigned long long)t);
-    }
-}
-
-// indirect form: gather the key through each object pointer (level 1: at off1; level 2: behind the
-// pointer held at off1, at off2; level 3: keys_in[i], supplied by the caller), write the filtered key
-template <typename U, int MODE, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__restrict__ ptrs, uint64_t n,
-                                                              uint32_t dmask, int64_t off1, int64_t off2, int level,
-                                                              const U *__restrict__ keys_in,
-                                                              U *__restrict__ keys_out,
-                                                              unsigned long long *__restrict__ ghist) {
-    constexpr int P = KeyTraits<U>::kDigits;
-    __shared__ uint32_t shall[gather_hist_copies<P>() * P * kBuckets];
-    zero_hist<THREADS, P>(shall);
-    uint32_t *sh = shall + ((threadIdx.x >> 5) % gather_hist_copies<P>()) * P * kBuckets;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t gwarp = (uint64_t(blockIdx.x) * THREADS + threadIdx.x) >> 5;
-    const uint64_t nwarps = (uint64_t(gridDim.x) * THREADS) >> 5;
-    constexpr int UNR = 4;
-    for (uint64_t b = gwarp * 32 * UNR; b < n; b += nwarps * 32 * UNR) {
-        U raw[UNR];
-#pragma unroll
-        for (int u = 0; u < UNR; ++u) {
-            const uint64_t i = b + u * 32 + lane;
-            raw[u] = U{};
-            if (i < n) {
-                if (level == 3) {
-                    raw[u] = keys_in[i];
-                } else {
-                    const unsigned char *obj = reinterpret_cast<const unsigned char *>(ptrs[i]) + off1;
-                    if (level == 2) obj = load_ptr(obj) + off2;
-                    raw[u] = load_member<U>(obj);
-                }
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < UNR; ++u) {
-            const uint64_t i = b + u * 32 + lane;
-            const bool ok = i < n;
-            // the stored key is final: filtered, and complemented for descending sorts
-            const U k = dmask ? key_not(filter_key<MODE>(raw[u])) : filter_key<MODE>(raw[u]);
-            if (ok) keys_out[i] = k;
-            count_key(sh, k, ok, 0u);
-        }
-    }
-    flush_hist<THREADS, P>(shall, ghist);
-}
 
 // ---- scan, pass-skip and plan -----------------------------------------------------------------
 
@@ -195,7 +46,17 @@ struct PlanArgs {
 // pass 1.13 ms -> 1.05 ms at 2^28 keys with the fullest digit ranked by ballots, 1.13 ms with both)
 constexpr unsigned long long kHotShare = 4;
 
-// the largest value over the 256 threads of k_plan (all threads call it)
+// the plan's 256 threads (one per digit) meet at named barrier 1, so the rest of the block that runs
+// the plan can leave
+__device__ __forceinline__ void plan_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ int plan_sync_or(int pred) {
+    int r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, 1, 256, p;\n\t"
+                 "selp.s32 %0, 1, 0, q;\n\t}" : "=r"(r) : "r"(pred) : "memory");
+    return r;
+}
+
+// the largest value over the plan's 8 warps (threads 0..255 call it)
 __device__ __forceinline__ unsigned long long plan_block_max(unsigned long long v, unsigned long long *wbuf) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -204,24 +65,28 @@ __device__ __forceinline__ unsigned long long plan_block_max(unsigned long long 
         v = y > v ? y : v;
     }
     if (lane == 0) wbuf[w] = v;
-    __syncthreads();
+    plan_sync();
     unsigned long long m = wbuf[0];
-    for (int i = 1; i < 8; ++i) m = wbuf[i] > m ? wbuf[i] : m;
-    __syncthreads();
+    for (int i = 1; i < kBuckets / 32; ++i) m = wbuf[i] > m ? wbuf[i] : m;
+    plan_sync();
     return m;
 }
 
-// one CTA of 256 threads
-static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
-                                              unsigned long long *__restrict__ bstart, uint64_t n, PlanArgs a) {
-    __shared__ unsigned long long wsum[8];
+// The plan of the sort from the complete digit histograms: bucket starts (exclusive scans), the
+// pass-skip test, the crowded digit of each pass and the ping-pong schedule.  Run by the last
+// histogram CTA to finish (so it needs no launch of its own): its threads 0..255, one per digit,
+// call it; the block's other threads do not.
+__device__ __forceinline__ void plan_body(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
+                                          unsigned long long *__restrict__ bstart, uint64_t n, const PlanArgs &a) {
+    __shared__ unsigned long long wsum[kBuckets / 32];
     __shared__ int skip[kMaxPasses];
     __shared__ uint32_t hot[kMaxPasses];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     for (int p = 0; p < int(a.passes); ++p) {
-        const unsigned long long h = ghist[p * kBuckets + t];
+        // the other CTAs' counts arrive through L2 (their atomics were fenced before they finished)
+        const unsigned long long h = __ldcg(ghist + p * kBuckets + t);
         // pass-skip: one bucket holds every key (Radixsortbidi8.hpp:12259, :12272, :2903)
-        const int all_in_one = __syncthreads_or(h == n);
+        const int all_in_one = plan_sync_or(h == n);
         // the pass's fullest bucket, (count << 8) | digit: a crowded one is ranked with ballots
         const unsigned long long m0 = plan_block_max((h << 8) | uint32_t(t), wsum);
         if (t == 0) {
@@ -235,12 +100,12 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
             if (lane >= o) x += y;
         }
         if (lane == 31) wsum[w] = x;
-        __syncthreads();
+        plan_sync();
         unsigned long long before = 0;
         for (int i = 0; i < w; ++i) before += wsum[i];
         bstart[p * kBuckets + t] = before + x - h;
         if (t == 0) skip[p] = all_in_one;
-        __syncthreads();
+        plan_sync();
     }
     if (t != 0) return;
     int k = 0;
@@ -296,6 +161,228 @@ static __global__ void __launch_bounds__(256) k_plan(Control *__restrict__ ctrl,
             ctrl->copy_dst = target;
         }
     }
+}
+
+// ---- up-front histograms --------------------------------------------------------------------
+
+// Gather-histogram counting: each CTA keeps kHistCopies sub-histograms (P digits x 256 bins, u32)
+// in shared memory and its warps spread over them, so warps rarely collide on a bin.  A warp whose
+// lanes all share the digit (a skewed digit, e.g. the zero top bytes of small keys) adds 32 with
+// one atomic instead of 32 conflicting ones.
+constexpr int kHistCopies = 4;
+
+__device__ __forceinline__ void hist_add(uint32_t *h, uint32_t d, bool valid) {
+    const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+    const bool v0 = __shfl_sync(0xFFFFFFFFu, valid, 0);
+    if (__all_sync(0xFFFFFFFFu, valid && d == d0)) {
+        if ((threadIdx.x & 31u) == 0 && v0) atomicAdd(h + d0, 32u);
+    } else if (valid) {
+        atomicAdd(h + d, 1u);
+    }
+}
+
+template <typename U>
+__device__ __forceinline__ void count_key(uint32_t *sh, U k, bool valid, uint32_t dmask) {
+#pragma unroll
+    for (int p = 0; p < KeyTraits<U>::kDigits; ++p) hist_add(sh + p * kBuckets, digit_of(k, p) ^ dmask, valid);
+}
+
+// copies of the gather histogram: fewer for the 16 digits of 128-bit keys (static shared memory)
+template <int P>
+constexpr int gather_hist_copies() { return P > 8 ? 2 : kHistCopies; }
+
+template <int THREADS, int P>
+__device__ __forceinline__ void zero_hist(uint32_t *sh) {
+    for (int i = threadIdx.x; i < gather_hist_copies<P>() * P * kBuckets; i += THREADS) sh[i] = 0;
+    __syncthreads();
+}
+
+template <int THREADS, int P>
+__device__ __forceinline__ void flush_hist(const uint32_t *sh, unsigned long long *ghist) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int c = 0; c < gather_hist_copies<P>(); ++c) v += sh[c * P * kBuckets + i];
+        if (v) atomicAdd(ghist + i, (unsigned long long)v);
+    }
+}
+
+// The CTA that finishes its share of the histograms last computes the plan (plan_body): each CTA
+// fences its global-histogram atomics before it counts itself done.  Every thread calls this.
+template <int THREADS>
+__device__ __forceinline__ void plan_if_last(Control *__restrict__ ctrl, const unsigned long long *__restrict__ ghist,
+                                             unsigned long long *__restrict__ bstart, uint64_t n, const PlanArgs &a) {
+    static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "the plan needs a thread per digit");
+    __shared__ uint32_t last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&ctrl->hist_done, 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!last || threadIdx.x >= kBuckets) return;
+    __threadfence();
+    plan_body(ctrl, ghist, bstart, n, a);
+}
+
+// Direct keys: all P digit histograms in one read.  Every (digit position, bin) has C shared-memory
+// counters, one per lane class (lane % C), laid out so that lane l always uses bank l % 32: the 32
+// lanes of a warp never meet in a bank (C = 32, keys up to 4 bytes) or at most pairwise (C = 16,
+// 8-byte keys, 128 KB either way).  One 1024-thread CTA per SM reads 16-byte vectors grid-strided;
+// at the end each CTA folds its C copies (rotated reads, conflict-free) into the global histogram.
+template <int P>
+constexpr int hist_lane_copies() { return P <= 4 ? 32 : (P <= 8 ? 16 : 8); }
+
+template <typename U, int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_histogram(const U *__restrict__ keys, uint64_t n, uint32_t dmask,
+                                                       unsigned long long *__restrict__ ghist, Control *__restrict__ ctrl,
+                                                       unsigned long long *__restrict__ bstart, PlanArgs pa) {
+    constexpr int P = KeyTraits<U>::kDigits;
+    constexpr int C = hist_lane_copies<P>();
+    constexpr int V = 16 / int(sizeof(U));
+    extern __shared__ __align__(16) uint32_t shl[];
+    for (int i = threadIdx.x; i < C * P * kBuckets; i += THREADS) shl[i] = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t *sh = shl + (lane & uint32_t(C - 1));
+    auto count = [&](U k, bool ok) {
+        if (!ok) return;
+#pragma unroll
+        for (int p = 0; p < P; ++p) atomicAdd(sh + (p * kBuckets + (digit_of(k, p) ^ dmask)) * C, 1u);
+    };
+    const uint64_t mis = (reinterpret_cast<uintptr_t>(keys) & 15u) / sizeof(U);
+    const uint64_t head = mis ? (uint64_t(V) - mis < n ? uint64_t(V) - mis : n) : 0;
+    const uint64_t nvec = (n - head) / V;
+    const uint64_t tail0 = head + nvec * V;
+    const uint64_t gthread = uint64_t(blockIdx.x) * THREADS + threadIdx.x;
+    const uint64_t nthreads = uint64_t(gridDim.x) * THREADS;
+    if (gthread < 32) {
+        for (uint64_t i = gthread; i < head; i += 32) count(filter_key<MODE>(keys[i]), true);
+        for (uint64_t i = tail0 + gthread; i < n; i += 32) count(filter_key<MODE>(keys[i]), true);
+    }
+    const uint4 *kv = reinterpret_cast<const uint4 *>(keys + head);
+    constexpr int UNR = 4;
+    for (uint64_t b = gthread; b < nvec; b += nthreads * UNR) {
+        uint4 v[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const uint64_t i = b + uint64_t(u) * nthreads;
+            v[u] = i < nvec ? __ldg(kv + i) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const bool ok = b + uint64_t(u) * nthreads < nvec;
+            U k[V];
+            memcpy(k, &v[u], 16);
+#pragma unroll
+            for (int j = 0; j < V; ++j) count(filter_key<MODE>(k[j]), ok);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < P * kBuckets; i += THREADS) {
+        uint32_t t = 0;
+#pragma unroll 8
+        for (int c = 0; c < C; ++c) t += shl[i * C + ((c + i) & (C - 1))];
+        if (t) atomicAdd(ghist + i, (unsigned long long)t);
+    }
+    plan_if_last<THREADS>(ctrl, ghist, bstart, n, pa);
+}
+
+// indirect form: gather the key through each object pointer (level 1: at off1; level 2: behind the
+// pointer held at off1, at off2; level 3: keys_in[i], supplied by the caller), write the filtered key
+template <typename U, int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_gather_histogram(const uint64_t *__restrict__ ptrs, uint64_t n,
+                                                              uint32_t dmask, int64_t off1, int64_t off2, int level,
+                                                              const U *__restrict__ keys_in,
+                                                              U *__restrict__ keys_out,
+                                                              unsigned long long *__restrict__ ghist,
+                                                              Control *__restrict__ ctrl,
+                                                              unsigned long long *__restrict__ bstart, PlanArgs pa) {
+    constexpr int P = KeyTraits<U>::kDigits;
+    __shared__ uint32_t shall[gather_hist_copies<P>() * P * kBuckets];
+    zero_hist<THREADS, P>(shall);
+    uint32_t *sh = shall + ((threadIdx.x >> 5) % gather_hist_copies<P>()) * P * kBuckets;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t gwarp = (uint64_t(blockIdx.x) * THREADS + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * THREADS) >> 5;
+    constexpr int UNR = 4;
+    for (uint64_t b = gwarp * 32 * UNR; b < n; b += nwarps * 32 * UNR) {
+        U raw[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const uint64_t i = b + u * 32 + lane;
+            raw[u] = U{};
+            if (i < n) {
+                if (level == 3) {
+                    raw[u] = keys_in[i];
+                } else {
+                    const unsigned char *obj = reinterpret_cast<const unsigned char *>(ptrs[i]) + off1;
+                    if (level == 2) obj = load_ptr(obj) + off2;
+                    raw[u] = load_member<U>(obj);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const uint64_t i = b + u * 32 + lane;
+            const bool ok = i < n;
+            // the stored key is final: filtered, and complemented for descending sorts
+            const U k = dmask ? key_not(filter_key<MODE>(raw[u])) : filter_key<MODE>(raw[u]);
+            if (ok) keys_out[i] = k;
+            count_key(sh, k, ok, 0u);
+        }
+    }
+    flush_hist<THREADS, P>(shall, ghist);
+    plan_if_last<THREADS>(ctrl, ghist, bstart, n, pa);
+}
+
+// ---- copy step --------------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ void copy_elems(const Control &c, const T *src, T *dst, uint64_t n) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c.copy_mode == kCopyPlain) {
+        for (uint64_t i = i0; i < n; i += stride) dst[i] = src[i];
+    } else if (c.copy_mode == kCopyReversed) {
+        for (uint64_t i = i0; i < n; i += stride) dst[i] = src[n - 1u - i];
+    } else if (c.copy_mode == kReverseInPlace) {
+        for (uint64_t i = i0; i < n / 2u; i += stride) {
+            const T a = dst[i], b = dst[n - 1u - i];
+            dst[i] = b;
+            dst[n - 1u - i] = a;
+        }
+    }
+}
+
+// the copy step: plain or reversed copy (or reversal in place) of n elements of elem_bytes bytes,
+// as the plan in the control block names it; every thread of the grid calls it.  elem_bytes and the
+// arrays are kernel parameters, like everything that sizes or addresses an access.
+__device__ __forceinline__ void copy_step(Control *__restrict__ ctrl, const SortArrays &arrs, uint64_t n,
+                                          uint32_t elem_bytes) {
+    const Control c = *ctrl;
+    if (c.copy_mode == kCopyNone) return;
+    bool bad = false;
+    const void *src = sort_array(arrs, c.copy_src, kArrIn, &bad);
+    void *dst = sort_array(arrs, c.copy_dst, kArrBuf, &bad);
+    if (bad || !src || !dst) {      // a damaged control block
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctrl->error, kDevFault);
+        return;
+    }
+    switch (elem_bytes) {
+        case 1: copy_elems<uint8_t>(c, static_cast<const uint8_t *>(src), static_cast<uint8_t *>(dst), n); break;
+        case 2: copy_elems<uint16_t>(c, static_cast<const uint16_t *>(src), static_cast<uint16_t *>(dst), n); break;
+        case 4: copy_elems<uint32_t>(c, static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst), n); break;
+        case 8: copy_elems<uint64_t>(c, static_cast<const uint64_t *>(src), static_cast<uint64_t *>(dst), n); break;
+        default:                   // 16-byte elements
+            copy_elems<uint4>(c, static_cast<const uint4 *>(src), static_cast<uint4 *>(dst), n);
+            break;
+    }
+}
+
+// the copy step of the in-place forms, after the last pass
+static __global__ void __launch_bounds__(256) k_copy(Control *__restrict__ ctrl, const SortArrays arrs, uint64_t n,
+                                                     uint32_t elem_bytes) {
+    copy_step(ctrl, arrs, n, elem_bytes);
 }
 
 // ---- the onesweep scatter pass ----------------------------------------------------------------
@@ -797,13 +884,17 @@ __device__ __forceinline__ void onesweep_body(unsigned char *smem, Control *__re
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, onesweep_min_blocks<U, HAS_VAL, THREADS>())
     k_onesweep(Control *__restrict__ ctrl, const SortArrays arrs, const unsigned long long *__restrict__ bstart_all,
-               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+               S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask, uint32_t fold_copy) {
     using L = OnesweepSmem<U, HAS_VAL, THREADS, ITEMS>;
     static_assert(THREADS >= kBuckets && THREADS % 32 == 0, "one thread per digit");
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     extern __shared__ __align__(16) unsigned char smem[];
     const PassPlan plan = ctrl->plan[pass];
-    if (!plan.active) return;
+    if (!plan.active) {
+        // the last pass of a copy form: when every pass was skipped, the copy the plan asks for
+        if (fold_copy) copy_step(ctrl, arrs, n, HAS_VAL ? 8u : uint32_t(sizeof(U)));
+        return;
+    }
     // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
     if (plan.hot == kNoHotPair)
         onesweep_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, arrs, bstart_all, status, pass, n, num_tiles,
@@ -1049,12 +1140,17 @@ __device__ __forceinline__ void onesweep_pipe_body(unsigned char *smem, Control 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 __global__ void __launch_bounds__(THREADS, 2)
     k_onesweep_pipe(Control *__restrict__ ctrl, const SortArrays arrs, const unsigned long long *__restrict__ bstart_all,
-                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask) {
+                    S *__restrict__ status, int pass, uint64_t n, uint32_t num_tiles, uint32_t dmask,
+                    uint32_t fold_copy) {
     static_assert(THREADS == 2 * kBuckets, "threads 0..255 scan, threads 256..511 look back");
     static_assert(PipeSmem<U, THREADS, ITEMS, HAS_VAL>::kTile <= 65535, "tile ranks are 16-bit");
     extern __shared__ __align__(16) unsigned char smem[];
     const PassPlan plan = ctrl->plan[pass];
-    if (!plan.active) return;
+    if (!plan.active) {
+        // the last pass of a copy form: when every pass was skipped, the copy the plan asks for
+        if (fold_copy) copy_step(ctrl, arrs, n, HAS_VAL ? 8u : uint32_t(sizeof(U)));
+        return;
+    }
     // a crowded pass ranks its hot digits with ballots (the choice is uniform over the launch)
     if (plan.hot == kNoHotPair)
         onesweep_pipe_body<U, MODE, HAS_VAL, THREADS, ITEMS, S, 0>(smem, ctrl, plan, arrs, bstart_all, status, pass, n,
@@ -1064,47 +1160,5 @@ __global__ void __launch_bounds__(THREADS, 2)
                                                                    num_tiles, dmask);
 }
 
-
-// ---- copy step --------------------------------------------------------------------------------
-
-template <typename T>
-__device__ __forceinline__ void copy_elems(const Control &c, const T *src, T *dst, uint64_t n) {
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    const uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c.copy_mode == kCopyPlain) {
-        for (uint64_t i = i0; i < n; i += stride) dst[i] = src[i];
-    } else if (c.copy_mode == kCopyReversed) {
-        for (uint64_t i = i0; i < n; i += stride) dst[i] = src[n - 1u - i];
-    } else if (c.copy_mode == kReverseInPlace) {
-        for (uint64_t i = i0; i < n / 2u; i += stride) {
-            const T a = dst[i], b = dst[n - 1u - i];
-            dst[i] = b;
-            dst[n - 1u - i] = a;
-        }
-    }
-}
-
-// the copy step; elem_bytes (a kernel parameter, like the arrays) is the size of one element
-static __global__ void __launch_bounds__(256) k_copy(Control *__restrict__ ctrl, const SortArrays arrs, uint64_t n,
-                                                     uint32_t elem_bytes) {
-    const Control c = *ctrl;
-    if (c.copy_mode == kCopyNone) return;
-    bool bad = false;
-    const void *src = sort_array(arrs, c.copy_src, kArrIn, &bad);
-    void *dst = sort_array(arrs, c.copy_dst, kArrBuf, &bad);
-    if (bad || !src || !dst) {      // a damaged control block
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctrl->error, kDevFault);
-        return;
-    }
-    switch (elem_bytes) {
-        case 1: copy_elems<uint8_t>(c, static_cast<const uint8_t *>(src), static_cast<uint8_t *>(dst), n); break;
-        case 2: copy_elems<uint16_t>(c, static_cast<const uint16_t *>(src), static_cast<uint16_t *>(dst), n); break;
-        case 4: copy_elems<uint32_t>(c, static_cast<const uint32_t *>(src), static_cast<uint32_t *>(dst), n); break;
-        case 8: copy_elems<uint64_t>(c, static_cast<const uint64_t *>(src), static_cast<uint64_t *>(dst), n); break;
-        default:                   // 16-byte elements
-            copy_elems<uint4>(c, static_cast<const uint4 *>(src), static_cast<uint4 *>(dst), n);
-            break;
-    }
-}
 
 }  // namespace rsbd8g

@@ -1,10 +1,12 @@
 // rsbd8g_launch.cuh - host-side launch sequence of one sort, templated on the key size; each
 // rsbd8g_sort_k*.cu instantiates it for one key size so the kernels compile in parallel.
 //
-//   memset(control, histograms, look-back state) -> histogram (or gather + histogram)
-//   -> plan (scan + pass-skip + ping-pong) -> one onesweep pass per digit -> copy step
+//   memset(control, histograms, look-back state) -> histogram (or gather + histogram), whose last
+//   CTA to finish writes the plan (scan + pass-skip + ping-pong) -> one onesweep pass per digit,
+//   the last of which also runs the copy step of the copy forms -> copy step (in-place forms only)
 // all on the caller's stream, with no host synchronisation in between (a skipped pass returns at
-// once on the device), so the sequence can be captured in a CUDA graph.
+// once on the device), so the sequence can be captured in a CUDA graph: 2 + digits launches for
+// the copy forms, 3 + digits for the in-place forms.
 #pragma once
 #include <algorithm>
 #include <mutex>
@@ -50,7 +52,7 @@ struct SweepKernels {
 
 template <typename U, int MODE, bool HAS_VAL, int THREADS, int ITEMS, typename S>
 cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsigned char *scratch,
-                            const SortArrays &arrs, uint32_t dmask, cudaStream_t s) {
+                            const SortArrays &arrs, uint32_t dmask, bool fold_copy, cudaStream_t s) {
     // the pipelined pass, unless there are too few tiles to fill its pipeline (a sort of about one
     // tile per CTA runs each tile's phases back to back in k_onesweep instead)
     using K = SweepKernels<U, MODE, HAS_VAL, THREADS, ITEMS, S>;
@@ -70,10 +72,11 @@ cudaError_t launch_sweeps_t(uint32_t passes, uint64_t n, const Layout &L, unsign
     for (uint32_t p = 0; p < passes; ++p) {
         S *status = reinterpret_cast<S *>(scratch + L.status + size_t(p) * L.status_pass_bytes);
         LaunchTimer t(s, RSBD8G_KERNEL_ONESWEEP, uint32_t(sizeof(U)), p, n);
+        const uint32_t fc = (fold_copy && p + 1 == passes) ? 1u : 0u;   // the copy forms' copy, in the last pass
         if (pipe)
-            pkern<<<grid, THREADS, PM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask);
+            pkern<<<grid, THREADS, PM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask, fc);
         else
-            kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask);
+            kern<<<grid, THREADS, SM::kBytes, s>>>(ctrl, arrs, bstart, status, int(p), n, L.num_tiles, dmask, fc);
     }
     return cudaGetLastError();
 }
@@ -92,18 +95,20 @@ void histogram_setup(int dev) {
 
 template <typename U, int MODE>
 cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, const Layout &L,
-                               unsigned char *scratch, uint32_t dmask, cudaStream_t s) {
+                               unsigned char *scratch, uint32_t dmask, const PlanArgs &pa, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     const uint64_t per_cta = uint64_t(kHistThreads) * 64;   // keys per CTA sweep, to size the grid
     const uint32_t grid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per_cta - 1) / per_cta,
                                                                             uint64_t(device_sms(dev)) * 4)));
     unsigned long long *ghist = reinterpret_cast<unsigned long long *>(scratch + L.ghist);
+    Control *ctrl = reinterpret_cast<Control *>(scratch + L.ctrl);
+    unsigned long long *bstart = reinterpret_cast<unsigned long long *>(scratch + L.bstart);
     LaunchTimer t(s, RSBD8G_KERNEL_HISTOGRAM, uint32_t(sizeof(U)), 0, n);
     if (r.indirect) {
         k_gather_histogram<U, MODE, kHistThreads><<<grid, kHistThreads, 0, s>>>(
             static_cast<const uint64_t *>(in), n, dmask, r.off1, r.off2, int(r.indirect),
-            static_cast<const U *>(r.keys), reinterpret_cast<U *>(scratch + L.keys_a), ghist);
+            static_cast<const U *>(r.keys), reinterpret_cast<U *>(scratch + L.keys_a), ghist, ctrl, bstart, pa);
     } else {
         constexpr int P = KeyTraits<U>::kDigits;
         constexpr size_t smem = size_t(hist_lane_copies<P>()) * P * kBuckets * 4;
@@ -111,7 +116,7 @@ cudaError_t launch_histogram_t(const Resolved &r, uint64_t n, const void *in, co
         histogram_setup<U, MODE>(dev);
         const uint64_t per = uint64_t(kHistDirectThreads) * 16;   // at least 16 keys a thread
         const uint32_t g = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + per - 1) / per, device_sms(dev))));
-        kern<<<g, kHistDirectThreads, smem, s>>>(static_cast<const U *>(in), n, dmask, ghist);
+        kern<<<g, kHistDirectThreads, smem, s>>>(static_cast<const U *>(in), n, dmask, ghist, ctrl, bstart, pa);
     }
     return cudaGetLastError();
 }
@@ -131,10 +136,6 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     if (e != cudaSuccess) return e;
     const int mode = int(r.f.absv | (r.f.sign << 1) | (r.f.fltp << 2));
     const uint32_t dmask = r.f.desc ? 0xFFu : 0u;
-#define RSBD8G_HIST(M) e = launch_histogram_t<U, M>(r, n, in, L, scratch, dmask, s)
-    RSBD8G_MODE_SWITCH(mode, RSBD8G_HIST)
-#undef RSBD8G_HIST
-    if (e != cudaSuccess) return e;
     SortArrays arrs{};
     arrs.p[kArrIn] = in;
     arrs.p[kArrOut] = out;
@@ -152,36 +153,35 @@ cudaError_t launch_sort_t(const Resolved &r, uint64_t n, const Layout &L, unsign
     const bool stall = (r.flags & RSBD8G_FLAG_DIAG_STALL) != 0;
     a.stall_tile = stall ? 1u : 0xFFFFFFFFu;
     a.spin_limit_ns = stall ? 200000000ull : 1000000000ull;
-    {
-        LaunchTimer t(s, RSBD8G_KERNEL_PLAN, uint32_t(sizeof(U)), 0, n);
-        k_plan<<<1, 256, 0, s>>>(reinterpret_cast<Control *>(scratch + L.ctrl),
-                                 reinterpret_cast<const unsigned long long *>(scratch + L.ghist),
-                                 reinterpret_cast<unsigned long long *>(scratch + L.bstart), n, a);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // the histograms; the CTA that finishes them last writes the plan
+#define RSBD8G_HIST(M) e = launch_histogram_t<U, M>(r, n, in, L, scratch, dmask, a, s)
+    RSBD8G_MODE_SWITCH(mode, RSBD8G_HIST)
+#undef RSBD8G_HIST
+    if (e != cudaSuccess) return e;
     const uint32_t P = uint32_t(KeyTraits<U>::kDigits);
     if (r.indirect) {
         e = L.wide_status
-                ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, arrs, 0u, s)
-                : launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint32_t>(P, n, L, scratch, arrs, 0u, s);
+                ? launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint64_t>(P, n, L, scratch, arrs, 0u, !inplace, s)
+                : launch_sweeps_t<U, 0, true, gi.threads, gi.items, uint32_t>(P, n, L, scratch, arrs, 0u, !inplace, s);
     } else if (L.wide_status) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint64_t>(P, n, L, scratch, arrs, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint64_t>(P, n, L, scratch, arrs, dmask, !inplace, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else if (L.large_tiles) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gl.threads, gl.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gl.threads, gl.items, uint32_t>(P, n, L, scratch, arrs, dmask, !inplace, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else if (L.small_tiles) {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gs.threads, gs.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gs.threads, gs.items, uint32_t>(P, n, L, scratch, arrs, dmask, !inplace, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     } else {
-#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint32_t>(P, n, L, scratch, arrs, dmask, s)
+#define RSBD8G_SWEEP(M) e = launch_sweeps_t<U, M, false, gd.threads, gd.items, uint32_t>(P, n, L, scratch, arrs, dmask, !inplace, s)
         RSBD8G_MODE_SWITCH(mode, RSBD8G_SWEEP)
 #undef RSBD8G_SWEEP
     }
     if (e != cudaSuccess) return e;
+    if (!inplace) return cudaSuccess;   // the copy forms' copy step ran in the last pass's launch
     int dev = 0;
     cudaGetDevice(&dev);
     const uint32_t cgrid = uint32_t(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(device_sms(dev)) * 8)));
@@ -211,7 +211,6 @@ cudaError_t prepare_mode_t(bool indirect, int dev) {
         SweepKernels<U, MODE, false, gl.threads, gl.items, uint32_t>::setup(dev, nullptr, nullptr);
         SweepKernels<U, MODE, false, gs.threads, gs.items, uint32_t>::setup(dev, nullptr, nullptr);
     }
-    cudaFuncGetAttributes(&fa, k_plan);
     cudaFuncGetAttributes(&fa, k_copy);
     return cudaGetLastError();
 }
