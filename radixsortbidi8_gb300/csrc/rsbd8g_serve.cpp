@@ -111,7 +111,7 @@ struct Batch {
     std::vector<Request *> reqs;
     int slot = -1;
     size_t scratch_off = 0, scratch_bytes = 0, tables_off = 0, tables_bytes = 0;
-    uint64_t *host_tables = nullptr;   // pinned: offsets, in, out, buf
+    unsigned char *host_tables = nullptr;   // pinned: offsets, in, out, buf, directions (device layout)
     uint32_t *host_err = nullptr;      // pinned: the device status word after the batch
     uint64_t keys = 0;
     double t_done = 0;
@@ -139,7 +139,7 @@ struct Server {
     Arena arena;
     std::vector<cudaStream_t> streams;
     std::vector<bool> slot_busy;
-    std::vector<uint64_t *> slot_tables;   // pinned staging per slot
+    std::vector<unsigned char *> slot_tables;   // pinned staging per slot, in the arena's table layout
     std::vector<uint32_t *> slot_err;
     size_t slot_table_cap = 0;
     uint32_t max_batch_requests = 4096;
@@ -322,8 +322,13 @@ struct Server {
     void issue(Batch *b) {
         const size_t n = b->reqs.size();
         rsbd8g_desc key = b->reqs.front()->desc;
-        uint64_t *ho = b->host_tables, *hi = ho + (n + 1), *hout = hi + n, *hbuf = hout + n;
-        uint8_t *hdir = reinterpret_cast<uint8_t *>(hbuf + n);
+        // the tables in the pinned slot buffer laid out as in the arena, so one copy moves them all
+        const size_t o_in = aup((n + 1) * 8), o_out = o_in + aup(n * 8), o_buf = o_out + aup(n * 8),
+                     o_dir = o_buf + aup(n * 8);
+        unsigned char *ht = b->host_tables;
+        uint64_t *ho = reinterpret_cast<uint64_t *>(ht), *hi = reinterpret_cast<uint64_t *>(ht + o_in),
+                 *hout = reinterpret_cast<uint64_t *>(ht + o_out), *hbuf = reinterpret_cast<uint64_t *>(ht + o_buf);
+        uint8_t *hdir = ht + o_dir;
         ho[0] = 0;
         // the buffers are in the arena (device memory): the batch may prefetch tiles into L2 when
         // every request's arrays are device memory too
@@ -339,10 +344,10 @@ struct Server {
         }
         unsigned char *dt = arena_base + b->tables_off;
         uint64_t *d_off = reinterpret_cast<uint64_t *>(dt);
-        uint64_t *d_in = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8));
-        uint64_t *d_out = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8) + aup(n * 8));
-        uint64_t *d_buf = reinterpret_cast<uint64_t *>(dt + aup((n + 1) * 8) + 2 * aup(n * 8));
-        uint8_t *d_dir = dt + aup((n + 1) * 8) + 3 * aup(n * 8);
+        uint64_t *d_in = reinterpret_cast<uint64_t *>(dt + o_in);
+        uint64_t *d_out = reinterpret_cast<uint64_t *>(dt + o_out);
+        uint64_t *d_buf = reinterpret_cast<uint64_t *>(dt + o_buf);
+        uint8_t *d_dir = dt + o_dir;
         cudaStream_t s = streams[size_t(b->slot)];
         rsbd8g_segtuning tun{1, 0, 0, 0};
         rsbd8g_status st = RSBD8G_OK;
@@ -353,12 +358,9 @@ struct Server {
             if (device) d.flags |= RSBD8G_FLAG_DEVICE_ARRAYS;
             st = rsbd8g_radixsortcopynoalloc(&d, r->count, arena_base + b->scratch_off, b->scratch_bytes, r->in, r->out,
                                              arena_base + r->buf_off, reinterpret_cast<rsbd8g_stream>(s));
-        } else if (cudaMemcpyAsync(d_off, ho, (n + 1) * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_in, hi, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_out, hout, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_buf, hbuf, n * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_dir, hdir, n, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        } else if (cudaMemcpyAsync(dt, ht, o_dir + n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
             st = RSBD8G_ERR_CUDA;
+        }
         else
             st = rsbd8g_segmented_sortcopy_ptrs_dirs(&key, b->keys, n, d_off, d_in, d_out, d_buf, d_dir,
                                                      arena_base + b->scratch_off, b->scratch_bytes, &tun,
@@ -422,10 +424,13 @@ RSBD8G_API rsbd8g_status rsbd8g_server_create(size_t budget_bytes, uint32_t max_
     s.slot_table_cap = s.max_batch_requests + 1;
     for (uint32_t i = 0; i < max_inflight; ++i) {
         cudaStream_t st;
-        uint64_t *tab = nullptr;
+        unsigned char *tab = nullptr;
         uint32_t *err = nullptr;
+        // a batch of n < slot_table_cap requests: offsets, three pointer tables and the directions,
+        // each starting on a 256-byte boundary as in the arena
+        const size_t tab_bytes = 4 * aup(s.slot_table_cap * 8) + aup(s.slot_table_cap);
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaMallocHost(reinterpret_cast<void **>(&tab), (s.slot_table_cap * 4 + 8) * 8 + s.slot_table_cap) != cudaSuccess ||
+            cudaMallocHost(reinterpret_cast<void **>(&tab), tab_bytes) != cudaSuccess ||
             cudaMallocHost(reinterpret_cast<void **>(&err), 64) != cudaSuccess) {
             cudaGetLastError();
             delete h;
