@@ -253,8 +253,7 @@ def gb300_arm(args, rank: int, world: int):
         # near the server's capacity (about 36 GKeys/s offered): requests queue, and the waiting
         # ones are coalesced into shared launches
         serving["near_capacity"] = serving_run(args, 6000.0, 2.0, 0, 0 if args.no_cpu else 8)
-    # correctness of the timed outputs: byte comparison with the oracle (the cpu_baseline leg's
-    # checker, outside the timed region)
+    # correctness of the timed outputs: byte comparison with the oracle, outside the timed region
     check = "not checked (--no-cpu)" if args.no_cpu else verify_outputs(arrays, bufs)
 
     ms_step = max_over_ranks(ms_total / args.steps, world, dev)
@@ -332,7 +331,7 @@ def gb300_arm(args, rank: int, world: int):
 
 
 def verify_outputs(arrays, bufs) -> str:
-    """The cpu_baseline leg's checker: each timed output copied to the host and compared byte for
+    """Verification of the timed outputs: each one copied to the host and compared byte for
     byte with the oracle's sort (the C restatement, all host threads) of the host copy of its input.
     Runs after the timed region."""
     from oracle import oracle as O
@@ -782,7 +781,7 @@ def config1_small(args, rs, dev, stream) -> dict:
             if i >= max(3, args.warmup):
                 times.append(e0.elapsed_time(e1))
     ms = statistics.median(times)
-    from oracle import oracle as O          # the checker
+    from oracle import oracle as O          # verifies the results, outside the timed region
     want = O.sortcopy(a, threads=oracle_threads())
     ok = np_bytes_equal(out.cpu().numpy().view(np.uint32), want)
     # the same sort captured once as a CUDA graph and replayed (the launch sequence has no host
@@ -847,7 +846,7 @@ def config3_records(args, rs, dev, stream, peak) -> dict:
     rec_h = np.ascontiguousarray(rec.cpu().numpy())
     del rec, ptrs, out, buf, scr
     torch.cuda.empty_cache()
-    from oracle import oracle as O          # the checker
+    from oracle import oracle as O          # verifies the results, outside the timed region
     hb = rec_h.ctypes.data
     hp = np.uint64(hb) + np.arange(n, dtype=np.uint64) * np.uint64(24)
     want = (O.sortcopy_indirect(hp, np.float64, 8, "native", "ascfwdorder", threads=oracle_threads())
@@ -904,7 +903,7 @@ def batched_run(args, which: str, steps: int, check: bool) -> dict:
     if check:
         got = sorter.output.cpu().numpy().view(kdt)
         a = keys.cpu().numpy().view(kdt)
-        from oracle import oracle as O          # the checker
+        from oracle import oracle as O          # verifies the results, outside the timed region
         want = O.sortcopy_segments(a, offs, "native", "ascfwdorder", threads=oracle_threads())
         res["checked"] = "every segment bit-exact vs oracle" if np_bytes_equal(got, want) else "FAILED vs oracle"
     del keys, off_t, sorter, loop_out
@@ -989,7 +988,7 @@ def serving_run(args, rate: float, duration: float, closed: int, checks: int) ->
     lat = serving.latency_summary(infos)
     # checks: results whose output region no later request of the same key type overwrote, against
     # the oracle
-    from oracle import oracle as O          # the checker
+    from oracle import oracle as O          # verifies the results, outside the timed region
     kk = np.array([m[0] for m in metas])
     pp = np.array([m[5] for m in metas], dtype=np.int64)
     nn = np.array([m[1] for m in metas], dtype=np.int64)

@@ -1,7 +1,7 @@
-"""The oracle: CPU checker for the GB300 radix sort (test infrastructure only).
+"""The oracle: the CPU restatement that verifies the GB300 radix sort (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import this module, and only as the checker (or as the timed
+``bench.py`` may import this module, and only to verify results (or as the timed
 CPU stand-in of the reference).  The product path never calls it.
 
 Three independent CPU opinions live here:

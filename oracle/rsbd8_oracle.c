@@ -2,7 +2,7 @@
  * rsbd8_oracle.c - the ORACLE for the GB300 radix sort.
  *
  * Test infrastructure only: the parity tests, the smoke check and the CPU
- * baseline leg of bench.py call this code as the checker (or as the timed
+ * baseline leg of bench.py call this code to verify results (or as the timed
  * CPU stand-in of the reference).  Nothing on the product path links it.
  *
  * It is a plain-C restatement of the stable LSD radix sort in
