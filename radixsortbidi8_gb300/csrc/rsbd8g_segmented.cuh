@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(THREADS, 2)
     using L = PipeSmem<U, THREADS, ITEMS>;
     static_assert(L::kTile <= 65535, "tile ranks are 16-bit");
     constexpr int TILE = L::kTile;
-    using R = TileRank<THREADS, ITEMS>;
+    using R = TileRank<THREADS, ITEMS, rank_lanes<ITEMS>(), sizeof(U) == 8>;   // dense ranks: 8-byte keys
     extern __shared__ __align__(16) unsigned char smem[];
     U *stage = reinterpret_cast<U *>(smem);
     uint32_t *utab = reinterpret_cast<uint32_t *>(smem + L::kOffUnits);
