@@ -66,6 +66,7 @@ def parse_args():
     p.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
     p.add_argument("--rate", type=float, default=2000.0, help="serving: requests per second")
     p.add_argument("--batch-scale", type=float, default=1.0, help="batched: fraction of the segment counts")
+    p.add_argument("--batches", default="A_2p28,A,B", help="batched: which batches to run (comma-separated)")
     p.add_argument("--calibrate-cpu", action="store_true",
                    help="where the reference was compiled (oracle/_ref): time its sort beside the oracle's port "
                         "on the same host cores and inputs, and print the ratio")
@@ -914,7 +915,10 @@ def batched_run(args, which: str, steps: int, check: bool) -> dict:
 def batched_config(args) -> dict:
     """Batch A: 100,000 uint32 arrays, lengths log-uniform [16, 2^20] (seed 0x5EED0005), also truncated
     at a cumulative 2^28 keys; batch B: 20,000 float64 arrays, log-uniform [64, 2^18] (seed 0x5EED0006)."""
-    res = {w: batched_run(args, w, args.steps, check=not args.no_cpu) for w in ("A_2p28", "A", "B")}
+    which = [w for w in args.batches.split(",") if w]
+    if not which or any(w not in ("A_2p28", "A", "B") for w in which):
+        raise SystemExit(f"--batches: a comma-separated subset of A_2p28, A, B, not {args.batches!r}")
+    res = {w: batched_run(args, w, args.steps, check=not args.no_cpu) for w in which}
     return {"config": "batched segmented sort (one captured CUDA graph per batch) vs per-array loop",
             "steps": args.steps, "results": res}
 
