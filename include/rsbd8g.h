@@ -318,6 +318,9 @@ RSBD8G_API const char *rsbd8g_status_string(rsbd8g_status status);
 
 /* ---- launch profiling (measurement support; no counterpart in the reference) ---------- */
 
+/* The plain sorts compute their plan in the histogram launch, so PLAN records only the segmented
+ * sort's plan launch. The copy forms fold the copy step into the last digit pass, so COPY records the
+ * in-place forms' copy launch and the segmented sort's. */
 enum {
     RSBD8G_KERNEL_MEMSET = 0, RSBD8G_KERNEL_HISTOGRAM = 1, RSBD8G_KERNEL_PLAN = 2,
     RSBD8G_KERNEL_ONESWEEP = 3, RSBD8G_KERNEL_COPY = 4, RSBD8G_KERNEL_SEGMENTED = 5, RSBD8G_KERNEL_MERGE = 6
