@@ -415,7 +415,7 @@ RSBD8G_API rsbd8g_status rsbd8g_scratch_status(void *scratch, rsbd8g_stream stre
 
 // The allocating forms draw buffer + scratch from a library-owned stream-ordered pool per device
 // that keeps up to kPoolKeepBytes of freed memory mapped, so back-to-back sorts do not map (and
-// the driver does not unmap) hundreds of megabytes on every call; the process-wide default pool
+// the CUDA driver does not unmap) hundreds of megabytes on every call; the process-wide default pool
 // is left as the application configured it.
 constexpr uint64_t kPoolKeepBytes = uint64_t(8) << 30;
 
